@@ -1,0 +1,278 @@
+"""Host-side interface of the GB300 midpoint Lennard-Jones path.
+
+Mirrors the reference's force interface (SRC/exaMD_forces.f90:308-318):
+``forces_midpoint_all(pos, box, cutoff, ...)`` is the counterpart of
+``Call exaMD_forces_midpoint_all(lennardjones_12, cutoff, noprocs)`` with the
+module state (blocks, globalbox, prmvdw) passed explicitly, and, like the
+reference, accumulates into a caller-supplied force array.  ``MidpointLJ``
+keeps the atoms resident on the GPU for repeated calls, velocity-Verlet runs
+and batched ensembles.  Everything goes through the C ABI of
+``include/examd_gb300.h``; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import weakref
+
+import numpy as np
+
+from . import _lib as _L
+from ._lib import ExamdError, check
+
+__all__ = ["MidpointLJ", "forces_midpoint_all", "gen_fcc", "gen_velocities", "gen_random", "gen_jittered_sc",
+           "pinned_empty", "own_table", "ExamdError", "FP64", "MIXED"]
+
+FP64 = "fp64"
+MIXED = "mixed"
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _table(v, nt):
+    a = np.asarray(v, dtype=np.float64)
+    if a.ndim == 0:
+        a = np.full((nt, nt), float(a))
+    return np.ascontiguousarray(a.reshape(nt, nt))
+
+
+class MidpointLJ:
+    """Resident GPU state for one box or a batch of independent boxes.
+
+    boxes: (nboxes, 3) box edges (or one 3-vector); natoms: atoms per box.
+    precision: "fp64" (FP64 end to end) or "mixed" (FP32 pair forces, FP64
+    positions, integration and reductions).  eps/sigma/rc: scalars or
+    (ntypes, ntypes) tables; block_length defaults to max(rc)/2 as the
+    reference (exaMD.f90:56)."""
+
+    def __init__(self, boxes, natoms, *, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None,
+                 block_length=None, tile=None, warps=None, strict_box=False, device=0):
+        lib = _L.load()
+        self._lib = lib
+        b = np.atleast_2d(np.asarray(boxes, dtype=np.float64))
+        n = np.atleast_1d(np.asarray(natoms, dtype=np.int64))
+        if b.shape[1] != 3 or b.shape[0] != n.shape[0]:
+            raise ValueError("boxes must be (nboxes, 3) with one natoms per box")
+        self.nboxes = int(b.shape[0])
+        self.natoms = n.copy()
+        self.n = int(n.sum())
+        self.box_edges = b.copy()
+        p = _L.Params()
+        lib.examd_default_params(C.byref(p))
+        p.precision = _L.FP64 if precision == FP64 else _L.MIXED
+        if precision not in (FP64, MIXED):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
+        p.ntypes = int(ntypes)
+        e, s, r = _table(eps, ntypes), _table(sigma, ntypes), _table(rc, ntypes)
+        for k in range(ntypes * ntypes):
+            p.eps[k] = e.flat[k]
+            p.sigma[k] = s.flat[k]
+            p.rc[k] = r.flat[k]
+        m = np.ones(ntypes) if mass is None else np.broadcast_to(np.asarray(mass, dtype=np.float64), (ntypes,))
+        for k in range(ntypes):
+            p.mass[k] = m[k]
+        self.mass = np.array(m, dtype=np.float64)
+        p.cell_edge = 0.0 if block_length is None else float(block_length)
+        if tile is not None:
+            for a in range(3):
+                p.tile[a] = int(tile[a] if np.ndim(tile) else tile)
+        p.warps = 0 if warps is None else int(warps)
+        p.strict_box = 1 if strict_box else 0
+        p.device = int(device)
+        self.params = p
+        arr = (_L.Box * self.nboxes)()
+        for k in range(self.nboxes):
+            for a in range(3):
+                arr[k].L[a] = b[k, a]
+            arr[k].natoms = int(n[k])
+        ctx = C.c_void_p()
+        check(lib.examd_gpu_create(C.byref(p), self.nboxes, arr, C.byref(ctx)), "examd_gpu_create")
+        self._ctx = ctx
+        self._fin = weakref.finalize(self, lib.examd_gpu_destroy, ctx)
+        self.types = None
+
+    # -- lifecycle -----------------------------------------------------------
+    def close(self):
+        if self._fin.alive:
+            self._fin()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _chk(self, code, where):
+        check(code, where, self._ctx)
+
+    # -- atoms ---------------------------------------------------------------
+    def set_atoms(self, pos, types=None, vel=None):
+        """pos: (n, 3) in posn(3,n) order, boxes concatenated."""
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        if p.shape[0] != self.n:
+            raise ValueError(f"expected {self.n} atoms, got {p.shape[0]}")
+        t = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+        self.types = t
+        self._chk(self._lib.examd_gpu_set_atoms(self._ctx, self.n, _d(p), _i(t), _d(v)), "examd_gpu_set_atoms")
+
+    def forces(self, out=None, accumulate=False, energy=False):
+        """One force evaluation at the resident positions.
+
+        Returns (forces (n,3), epot per box, virial per box); epot/virial are
+        None unless energy=True.  With accumulate=True the forces are added to
+        ``out`` (the reference's += semantics)."""
+        f = out if out is not None else np.zeros((self.n, 3))
+        if f.dtype != np.float64 or not f.flags.c_contiguous or f.shape != (self.n, 3):
+            raise ValueError("out must be a C-contiguous (n, 3) float64 array")
+        ep = np.zeros(self.nboxes) if energy else None
+        w = np.zeros(self.nboxes) if energy else None
+        self._chk(self._lib.examd_gpu_forces(self._ctx, _d(f), _d(ep), _d(w), 1 if accumulate else 0),
+                  "examd_gpu_forces")
+        return f, ep, w
+
+    def forces_at(self, pos, out=None, accumulate=False, energy=False):
+        """New positions (same atoms, caller order) and one force evaluation."""
+        p = pos if (isinstance(pos, np.ndarray) and pos.dtype == np.float64 and pos.flags.c_contiguous) \
+            else np.ascontiguousarray(pos, dtype=np.float64)
+        f = out if out is not None else np.zeros((self.n, 3))
+        ep = np.zeros(self.nboxes) if energy else None
+        w = np.zeros(self.nboxes) if energy else None
+        self._chk(self._lib.examd_gpu_forces_at(self._ctx, _d(p), _d(f), _d(ep), _d(w), 1 if accumulate else 0),
+                  "examd_gpu_forces_at")
+        return f, ep, w
+
+    def run(self, nsteps, dt, graph_chunk=0, energies=False):
+        """Velocity-Verlet steps.  Returns dict(ms, ekin[steps, boxes], epot[steps, boxes])."""
+        en = np.zeros((max(nsteps, 1), self.nboxes, 2)) if energies else None
+        st = _L.Stats()
+        self._chk(self._lib.examd_gpu_run(self._ctx, int(nsteps), float(dt), int(graph_chunk), _d(en),
+                                          C.byref(st)), "examd_gpu_run")
+        out = dict(ms=st.ms, steps=st.steps)
+        if energies:
+            out["ekin"] = en[:nsteps, :, 0].copy()
+            out["epot"] = en[:nsteps, :, 1].copy()
+        return out
+
+    def state(self):
+        pos = np.zeros((self.n, 3))
+        vel = np.zeros((self.n, 3))
+        self._chk(self._lib.examd_gpu_get_state(self._ctx, _d(pos), _d(vel)), "examd_gpu_get_state")
+        return pos, vel
+
+    def kinetic(self):
+        ek = np.zeros(self.nboxes)
+        self._chk(self._lib.examd_gpu_kinetic(self._ctx, _d(ek)), "examd_gpu_kinetic")
+        return ek
+
+    def scale_velocities(self, factor):
+        f = np.ascontiguousarray(np.broadcast_to(np.asarray(factor, dtype=np.float64), (self.nboxes,)))
+        self._chk(self._lib.examd_gpu_scale_velocities(self._ctx, _d(f)), "examd_gpu_scale_velocities")
+
+    def time_forces(self, reps):
+        """Device time (ms) of `reps` pair-kernel launches on the context stream; returns (total, per launch)."""
+        ms = C.c_double()
+        kms = C.c_double()
+        self._chk(self._lib.examd_gpu_time_forces(self._ctx, int(reps), C.byref(ms), C.byref(kms)),
+                  "examd_gpu_time_forces")
+        return ms.value, kms.value
+
+    def counters(self):
+        c, a, t, m = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        self._chk(self._lib.examd_gpu_counters(self._ctx, C.byref(c), C.byref(a), C.byref(t), C.byref(m)),
+                  "examd_gpu_counters")
+        return dict(candidates=c.value, accepted=a.value, tiles=t.value, max_tile_atoms=m.value)
+
+
+def forces_midpoint_all(pos, box, cutoff, eps=1.0, sigma=1.0, forces=None, precision=FP64, energy=False, **kw):
+    """One midpoint LJ force evaluation on the GPU for a single periodic box.
+
+    Counterpart of exaMD_forces_midpoint_all(lennardjones_12, cutoff, noprocs=1)
+    (SRC/exaMD_forces.f90:308-390) with prmvdw(1,:) = (eps, sigma, -, -, cutoff)
+    (exaMD.f90:199-202).  ``forces`` when given is accumulated into (+=), as the
+    reference accumulates into grid%forces.  Returns forces, or
+    (forces, epot, virial) when energy=True."""
+    p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    with MidpointLJ(np.asarray(box, dtype=np.float64).reshape(1, 3), [p.shape[0]], precision=precision, eps=eps,
+                    sigma=sigma, rc=cutoff, **kw) as sysm:
+        sysm.set_atoms(p)
+        if forces is None:
+            f, ep, w = sysm.forces(energy=energy)
+        else:
+            f, ep, w = sysm.forces(out=forces, accumulate=True, energy=energy)
+    return (f, float(ep[0]), float(w[0])) if energy else f
+
+
+# -- generators (host code in the library) ------------------------------------
+def gen_fcc(nc, rho):
+    """4*nc^3 atoms on an FCC lattice at density rho; returns (pos (n,3), L)."""
+    lib = _L.load()
+    pos = np.zeros((4 * nc ** 3, 3))
+    L = C.c_double()
+    check(lib.examd_gen_fcc(int(nc), float(rho), _d(pos), C.byref(L)), "examd_gen_fcc")
+    return pos, L.value
+
+
+def gen_velocities(n, T, seed, types=None, mass=None):
+    lib = _L.load()
+    v = np.zeros((n, 3))
+    t = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
+    m = None if mass is None else np.ascontiguousarray(mass, dtype=np.float64)
+    check(lib.examd_gen_velocities(int(n), _i(t), _d(m), float(T), C.c_uint64(seed), _d(v)), "examd_gen_velocities")
+    return v
+
+
+def gen_random(n, L, dmin, seed, lo=None, hi=None, fixed=None, max_tries=100000):
+    """Uniform random positions with minimum separation dmin (periodic).  ``fixed``:
+    already placed atoms kept in front; lo/hi: the region to fill."""
+    lib = _L.load()
+    L = np.asarray(L, dtype=np.float64).reshape(3)
+    lo = np.zeros(3) if lo is None else np.asarray(lo, dtype=np.float64).reshape(3)
+    hi = L.copy() if hi is None else np.asarray(hi, dtype=np.float64).reshape(3)
+    nf = 0 if fixed is None else len(fixed)
+    pos = np.zeros((nf + n, 3))
+    if nf:
+        pos[:nf] = fixed
+    check(lib.examd_gen_random(nf + n, nf, _d(np.ascontiguousarray(L)), _d(np.ascontiguousarray(lo)),
+                               _d(np.ascontiguousarray(hi)), float(dmin), C.c_uint64(seed), int(max_tries), _d(pos)),
+          "examd_gen_random")
+    return pos
+
+
+def gen_jittered_sc(m, rho, jitter, frac_b, seed):
+    lib = _L.load()
+    pos = np.zeros((m ** 3, 3))
+    t = np.zeros(m ** 3, dtype=np.int32)
+    L = C.c_double()
+    check(lib.examd_gen_jittered_sc(int(m), float(rho), float(jitter), float(frac_b), C.c_uint64(seed), _d(pos),
+                                    _i(t), C.byref(L)), "examd_gen_jittered_sc")
+    return pos, t, L.value
+
+
+def own_table():
+    """(rows (13,2), lut (125,13)) derived by the library from the 63-entry table."""
+    lib = _L.load()
+    rows = (C.c_byte * 26)()
+    lut = (C.c_ubyte * (125 * 13))()
+    check(lib.examd_own_table(rows, lut), "examd_own_table")
+    return (np.frombuffer(bytes(rows), dtype=np.int8).reshape(13, 2).copy(),
+            np.frombuffer(bytes(lut), dtype=np.uint8).reshape(125, 13).copy())
+
+
+def pinned_empty(shape, dtype=np.float64):
+    """numpy array in page-locked host memory (cudaHostAlloc), freed with the array."""
+    lib = _L.load()
+    n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    ptr = C.c_void_p()
+    check(lib.examd_host_alloc(C.byref(ptr), n), "examd_host_alloc")
+    buf = (C.c_byte * n).from_address(ptr.value)
+    arr = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+    weakref.finalize(buf, lib.examd_host_free, ptr)
+    arr.flags.writeable = True
+    return arr

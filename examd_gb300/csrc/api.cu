@@ -1,0 +1,1069 @@
+// api.cu -- the C ABI (include/examd_gb300.h): context, buffers, step
+// sequencing, CUDA-graph capture of the step loop.
+//
+// Host-side counterpart of the reference's setup and driver sequence:
+// exaMD_domain_create (SRC/exaMD_utils.f90:167-190), the neighbour-slot and
+// midpoint tables (SRC/exaMD_partitioning.f90:783-798,
+// SRC/exaMD_module.f90:276-346) and the timed force call (exaMD.f90:241-253).
+// The METIS partition of blocks over ranks (SRC/exaMD_partitioning.f90:65-455)
+// becomes a fixed partition of cells into CTA tiles.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+using namespace examd;
+
+namespace {
+
+// The 63 (slot_a, slot_b) block-pair classes of the midpoint method, slot =
+// (ii+1) + 3(jj+1) + 9(kk+1) + 1 with ii fastest, 14 = home.  This table is
+// the ownership rule itself, so it is carried as the same data
+// (SRC/exaMD_module.f90:282-344).
+const int kMidpointTable[63][2] = {
+    {14, 14}, {14, 15}, {14, 16}, {14, 17}, {14, 18}, {14, 19}, {14, 20}, {14, 21}, {14, 22},
+    {14, 23}, {14, 24}, {14, 25}, {14, 26}, {14, 27}, {10, 18}, {10, 27}, {11, 17}, {11, 18},
+    {11, 25}, {11, 26}, {11, 27}, {12, 16}, {12, 17}, {12, 25}, {13, 15}, {13, 18}, {13, 24},
+    {13, 27}, {15, 16}, {15, 19}, {15, 22}, {15, 25}, {16, 21}, {16, 24}, {17, 19}, {17, 20},
+    {17, 21}, {18, 19}, {19, 5},  {19, 9},  {20, 5},  {20, 7},  {20, 8},  {20, 9},  {21, 5},
+    {21, 7},  {22, 5},  {22, 6},  {22, 9},  {23, 5},  {24, 5},  {24, 4},  {24, 7},  {25, 5},
+    {25, 3},  {25, 6},  {26, 5},  {26, 2},  {26, 3},  {27, 1},  {27, 2},  {27, 4},  {27, 5}};
+
+void slot_offset(int s, int o[3]) {  // SRC/exaMD_partitioning.f90:786-795
+  s -= 1;
+  o[0] = s % 3 - 1;
+  o[1] = (s / 3) % 3 - 1;
+  o[2] = s / 9 - 1;
+}
+
+bool class_ok(int cls, int h) {  // home offset h keeps the home cell inside the tile
+  switch (cls) {
+    case 0: return h == 1;   // halo cell before the tile
+    case 1: return h >= 0;   // first cell
+    case 2: return true;     // interior
+    case 3: return h <= 0;   // last cell
+    default: return h == -1; // halo cell after the tile
+  }
+}
+
+// Derive the row structure and the per-class ownership masks from the table.
+// Returns false if the table does not have the expected shape.
+bool build_own_lut(OwnLut& L) {
+  std::memset(&L, 0, sizeof(L));
+  std::vector<std::pair<int, int>> rows;
+  std::map<std::pair<int, int>, std::map<int, std::array<int, 3>>> byrow;
+  for (int p = 1; p < 63; ++p) {
+    int a[3], b[3];
+    slot_offset(kMidpointTable[p][0], a);
+    slot_offset(kMidpointTable[p][1], b);
+    int d[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    auto key = std::make_pair(d[1], d[2]);
+    if (!byrow.count(key) && key != std::make_pair(0, 0)) rows.push_back(key);
+    if (byrow[key].count(d[0])) return false;  // duplicate separation
+    byrow[key][d[0]] = {-a[0], -a[1], -a[2]};  // home = A - slot_a
+  }
+  if (rows.size() != 12 || byrow.size() != 13) return false;
+  rows.push_back({0, 0});
+  for (int r = 0; r < kRows; ++r) {
+    L.rows[r][0] = (signed char)rows[r].first;
+    L.rows[r][1] = (signed char)rows[r].second;
+    const auto& m = byrow[rows[r]];
+    if (r < 12) {
+      if (m.size() != 5) return false;
+    } else if (m.size() != 2 || !m.count(1) || !m.count(2)) {
+      return false;
+    }
+  }
+  for (int cx = 0; cx < 5; ++cx)
+    for (int cy = 0; cy < 5; ++cy)
+      for (int cz = 0; cz < 5; ++cz) {
+        const int cls = cx * 25 + cy * 5 + cz;
+        for (int r = 0; r < kRows; ++r) {
+          unsigned mask = 0;
+          for (const auto& kv : byrow[rows[r]]) {
+            const auto& h = kv.second;
+            if (class_ok(cx, h[0]) && class_ok(cy, h[1]) && class_ok(cz, h[2])) mask |= 1u << (kv.first + 2);
+          }
+          if (r == kRows - 1 && class_ok(cx, 0) && class_ok(cy, 0) && class_ok(cz, 0)) mask |= 1u << 2;
+          L.lut[cls][r] = (unsigned char)mask;
+        }
+      }
+  return true;
+}
+
+int round_block_length(double want, double* out) {
+  if (!(want > 0.0) || !std::isfinite(want)) return EXAMD_ERR_ARG;
+  // largest k with ceil(want * 2^k) < 2^14: c * bl then needs <= 24 bits
+  int k = 13 - (int)std::floor(std::log2(want));
+  double bl = 0.0;
+  for (; k > -60; --k) {
+    double q = std::ceil(want * std::ldexp(1.0, k));
+    if (q < 16384.0) {
+      bl = std::ldexp(q, -k);
+      break;
+    }
+  }
+  if (!(bl >= want)) return EXAMD_ERR_ARG;
+  *out = bl;
+  return EXAMD_OK;
+}
+
+}  // namespace
+
+struct examd_ctx {
+  examd_params p{};
+  int nboxes = 0;
+  std::vector<examd_box> boxes;
+  std::vector<BoxDev> bh;
+  std::vector<int> tile0;  // nboxes + 1
+  std::vector<int64_t> atom0;
+  int64_t N = 0;
+  int NC = 0, ntiles = 0, ne_max = 0;
+  double bl = 0.0;
+  LJTable lj{};
+  PairConfig pc;
+  int cap = 0, smem = 0, smem_limit = 0;
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
+  std::string lasterr;
+
+  // device buffers
+  BoxDev* d_boxes = nullptr;
+  int4* d_tiles = nullptr;
+  int* d_tile0 = nullptr;
+  unsigned char* d_bmask = nullptr;
+  double* X[2][3] = {};
+  double* V[2][3] = {};
+  int* meta[2] = {};
+  int* id[2] = {};
+  int cur = 0;
+  float4* U = nullptr;
+  float4* Uold = nullptr;
+  int* cellS = nullptr;
+  int* cellOld = nullptr;
+  int* slot = nullptr;
+  int* src = nullptr;
+  int* count = nullptr;
+  int* cstart = nullptr;
+  int* bsum = nullptr;
+  int* d_total = nullptr;
+  void* Fown = nullptr;
+  void* P = nullptr;
+  double* tileE = nullptr;
+  double* tileW = nullptr;
+  long long* tileC = nullptr;
+  double* boxE = nullptr;  // per box (graph chunk: [chunk][nboxes])
+  double* boxW = nullptr;
+  double* boxKE = nullptr;
+  int* status = nullptr;
+  int* d_occ = nullptr;
+  double* stage = nullptr;   // 3N doubles (AoS I/O)
+  double* stage2 = nullptr;  // 3N doubles
+  int* d_meta_in = nullptr;
+  double* d_factor = nullptr;
+  int ebuf_steps = 0;
+
+  bool atoms_set = false;
+  bool forces_valid = false;  // Fown/P hold F(X[cur])
+  bool energy_valid = false;
+
+  // graph cache
+  cudaGraphExec_t gexec = nullptr;
+  int g_parity = -1, g_chunk = 0, g_energy = -1, g_cap = 0;
+  double g_dt = 0.0;
+
+  int cuda_fail(cudaError_t e, const char* what) {
+    lasterr = std::string(what) + ": " + cudaGetErrorString(e);
+    return EXAMD_ERR_CUDA;
+  }
+};
+
+#define CK(call)                                                    \
+  do {                                                              \
+    cudaError_t _e = (call);                                        \
+    if (_e != cudaSuccess) return ctx->cuda_fail(_e, #call);        \
+  } while (0)
+
+namespace {
+
+template <class T>
+int dalloc(examd_ctx* ctx, T** p, size_t count) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    ctx->lasterr = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    *p = nullptr;
+    return EXAMD_ERR_NOMEM;
+  }
+  return EXAMD_OK;
+}
+
+void free_all(examd_ctx* ctx) {
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  ctx->gexec = nullptr;
+  void* ptrs[] = {ctx->d_boxes, ctx->d_tiles, ctx->d_tile0, ctx->d_bmask, ctx->U, ctx->Uold, ctx->cellS,
+                  ctx->cellOld, ctx->slot, ctx->src, ctx->count, ctx->cstart, ctx->bsum, ctx->d_total,
+                  ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
+                  ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  for (int b = 0; b < 2; ++b) {
+    for (int a = 0; a < 3; ++a) {
+      if (ctx->X[b][a]) cudaFree(ctx->X[b][a]);
+      if (ctx->V[b][a]) cudaFree(ctx->V[b][a]);
+    }
+    if (ctx->meta[b]) cudaFree(ctx->meta[b]);
+    if (ctx->id[b]) cudaFree(ctx->id[b]);
+  }
+  if (ctx->e0) cudaEventDestroy(ctx->e0);
+  if (ctx->e1) cudaEventDestroy(ctx->e1);
+  if (ctx->e2) cudaEventDestroy(ctx->e2);
+  if (ctx->e3) cudaEventDestroy(ctx->e3);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+}
+
+int status_to_code(int st) {
+  if (st & ST_NONFINITE) return EXAMD_ERR_NONFINITE;
+  if (st & ST_OUTSIDE) return EXAMD_ERR_OUTSIDE;
+  if (st & ST_OVERFLOW) return EXAMD_ERR_CELL_OVERFLOW;
+  if (st & ST_TIMEOUT) return EXAMD_ERR_TIMEOUT;
+  return EXAMD_OK;
+}
+
+// Largest staged-atom count of any tile (ext cells), for the smem capacity.
+__global__ void k_tile_occupancy(const int4* __restrict__ tiles, const BoxDev* __restrict__ boxes,
+                                 const int* __restrict__ cstart, int* __restrict__ occ) {
+  __shared__ int part[32];
+  const int tile = blockIdx.x;
+  const int4 t0 = tiles[2 * tile], t1 = tiles[2 * tile + 1];
+  const BoxDev& B = boxes[t0.x];
+  const int EX = t1.x + 2, EY = t1.y + 2, EZ = t1.z + 2, NE = EX * EY * EZ;
+  int s = 0;
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+    int lx = e % EX, rr = e / EX, ly = rr % EY, lz = rr / EY;
+    int g[3] = {t0.y + lx - 1, t0.z + ly - 1, t0.w + lz - 1};
+    for (int a = 0; a < 3; ++a) {
+      if (g[a] < 0) g[a] += B.nb[a];
+      if (g[a] >= B.nb[a]) g[a] -= B.nb[a];
+    }
+    int gc = B.cell0 + g[0] + B.nb[0] * (g[1] + B.nb[1] * g[2]);
+    s += cstart[gc + 1] - cstart[gc];
+  }
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    atomicMax(&occ[0], t);
+  }
+}
+
+}  // namespace
+
+// --------------------------------------------------------------------------
+extern "C" {
+
+void examd_default_params(examd_params* p) {
+  std::memset(p, 0, sizeof(*p));
+  p->precision = EXAMD_FP64;
+  p->ntypes = 1;
+  p->eps[0] = 1.0;
+  p->sigma[0] = 1.0;
+  p->rc[0] = 2.5;
+  p->mass[0] = 1.0;
+}
+
+const char* examd_gpu_strerror(int code) {
+  switch (code) {
+    case EXAMD_OK: return "ok";
+    case EXAMD_ERR_OUTSIDE: return "position outside the box (block number out of range)";
+    case EXAMD_ERR_ARG: return "invalid argument or parameter";
+    case EXAMD_ERR_NB_TOO_SMALL: return "fewer than 5 cells on an axis: the 63-entry table would count pairs twice";
+    case EXAMD_ERR_CELL_OVERFLOW: return "a tile holds more atoms than its shared-memory capacity";
+    case EXAMD_ERR_NONFINITE: return "non-finite position";
+    case EXAMD_ERR_TIMEOUT: return "a bounded device wait gave up";
+    case EXAMD_ERR_CUDA: return "CUDA runtime error";
+    case EXAMD_ERR_NOMEM: return "out of device or pinned memory";
+    case EXAMD_ERR_STATE: return "invalid call order";
+    case EXAMD_ERR_NO_DEVICE: return "no usable sm_103 CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char* examd_gpu_last_error(examd_ctx* ctx) { return ctx ? ctx->lasterr.c_str() : ""; }
+
+int examd_own_table(signed char* rows, unsigned char* lut) {
+  if (!rows || !lut) return EXAMD_ERR_ARG;
+  OwnLut L;
+  if (!build_own_lut(L)) return EXAMD_ERR_ARG;
+  std::memcpy(rows, L.rows, sizeof(L.rows));
+  std::memcpy(lut, L.lut, sizeof(L.lut));
+  return EXAMD_OK;
+}
+
+int examd_host_alloc(void** ptr, int64_t bytes) {
+  if (!ptr || bytes < 0) return EXAMD_ERR_ARG;
+  return cudaHostAlloc(ptr, (size_t)std::max<int64_t>(bytes, 1), cudaHostAllocDefault) == cudaSuccess
+             ? EXAMD_OK
+             : EXAMD_ERR_NOMEM;
+}
+int examd_host_free(void* ptr) { return cudaFreeHost(ptr) == cudaSuccess ? EXAMD_OK : EXAMD_ERR_CUDA; }
+
+int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* boxes, examd_ctx** out) {
+  if (!params || !boxes || !out || nboxes < 1) return EXAMD_ERR_ARG;
+  *out = nullptr;
+  const examd_params& p = *params;
+  if (p.ntypes < 1 || p.ntypes > EXAMD_MAX_TYPES) return EXAMD_ERR_ARG;
+  if (p.precision != EXAMD_FP64 && p.precision != EXAMD_MIXED) return EXAMD_ERR_ARG;
+  const int nt = p.ntypes;
+  double rcmax = 0.0;
+  for (int a = 0; a < nt; ++a)
+    for (int b = 0; b < nt; ++b) {
+      const int k = a * nt + b, kt = b * nt + a;
+      if (!(p.eps[k] > 0) || !(p.sigma[k] > 0) || !(p.rc[k] > 0)) return EXAMD_ERR_ARG;
+      if (p.eps[k] != p.eps[kt] || p.sigma[k] != p.sigma[kt] || p.rc[k] != p.rc[kt]) return EXAMD_ERR_ARG;
+      rcmax = std::max(rcmax, p.rc[k]);
+    }
+  double want = p.cell_edge > 0 ? p.cell_edge : 0.5 * rcmax;
+  if (want < 0.5 * rcmax) return EXAMD_ERR_ARG;
+  double bl;
+  if (round_block_length(want, &bl) != EXAMD_OK) return EXAMD_ERR_ARG;
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1 || p.device < 0 || p.device >= ndev)
+    return EXAMD_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, p.device) != cudaSuccess) return EXAMD_ERR_NO_DEVICE;
+  if (prop.major != 10 || prop.minor != 3) return EXAMD_ERR_NO_DEVICE;  // built for sm_103a only
+
+  examd_ctx* ctx = new examd_ctx();
+  ctx->p = p;
+  ctx->nboxes = nboxes;
+  ctx->boxes.assign(boxes, boxes + nboxes);
+  ctx->bl = bl;
+  ctx->dev = p.device;
+  ctx->smem_limit = (int)prop.sharedMemPerBlockOptin;
+  cudaSetDevice(ctx->dev);
+
+  // pair-kernel configuration
+  ctx->pc.fp64 = p.precision == EXAMD_FP64;
+  ctx->pc.multi = nt > 1;
+  ctx->pc.kahan = true;
+  ctx->pc.warps = p.warps > 0 ? p.warps : 8;
+  if (ctx->pc.warps < 4 || ctx->pc.warps > 8) {
+    delete ctx;
+    return EXAMD_ERR_ARG;
+  }
+  const int deftile = ctx->pc.fp64 ? 4 : 6;
+  int T[3];
+  for (int a = 0; a < 3; ++a) {
+    T[a] = p.tile[a] > 0 ? p.tile[a] : deftile;
+    if (T[a] < 2 || T[a] > 14) {
+      delete ctx;
+      return EXAMD_ERR_ARG;
+    }
+  }
+
+  // LJ tables
+  LJTable& lj = ctx->lj;
+  lj.nt = nt;
+  float rc2max = 0.f;
+  for (int k = 0; k < nt * nt; ++k) {
+    const double e = p.eps[k], s = p.sigma[k], r = p.rc[k];
+    lj.p64[k].sig2 = s * s;      // sig2 = prmvdw(1,2)**2   (user_func.f90:59)
+    lj.p64[k].eps24 = 24.0 * e;  // eps24 = twentyfour*eps  (user_func.f90:58)
+    lj.p64[k].eps4 = 4.0 * e;
+    lj.p64[k].rc2 = r * r;       // prmvdw(1,5)**2           (user_func.f90:52)
+    lj.p32[k].sig2 = (float)(s * s);
+    lj.p32[k].m24eps = (float)(-24.0 * e);
+    lj.p32[k].c4eps = (float)(4.0 * e);
+    lj.p32[k].rc2 = (float)(r * r);
+    rc2max = std::max(rc2max, lj.p32[k].rc2);
+  }
+  lj.rc2max = rc2max;
+  for (int a = 0; a < EXAMD_MAX_TYPES; ++a) {
+    double m = (a < nt && p.mass[a] > 0) ? p.mass[a] : 1.0;
+    lj.mass[a] = m;
+    lj.minv[a] = 1.0 / m;
+  }
+
+  // boxes, cells, tiles
+  std::vector<int4> tiles;
+  std::vector<unsigned char> bmask;
+  int cell0 = 0;
+  int64_t a0 = 0;
+  for (int b = 0; b < nboxes; ++b) {
+    const examd_box& X = boxes[b];
+    BoxDev B{};
+    if (X.natoms < 0) {
+      delete ctx;
+      return EXAMD_ERR_ARG;
+    }
+    for (int a = 0; a < 3; ++a) {
+      if (!(X.L[a] > 0) || !std::isfinite(X.L[a])) {
+        delete ctx;
+        return EXAMD_ERR_ARG;
+      }
+      B.L[a] = X.L[a];
+      B.Li[a] = 1.0 / X.L[a];  // globalboxi = one/globalbox (SRC/exaMD_utils.f90:188)
+      B.Lf[a] = (float)X.L[a];
+      double q = X.L[a] / bl;  // nblocks_xyz = Int(globalbox/block_length) (:179)
+      if (q < 5.0) {
+        delete ctx;
+        return EXAMD_ERR_NB_TOO_SMALL;
+      }
+      if (q >= 1024.0) {
+        delete ctx;
+        return EXAMD_ERR_ARG;
+      }
+      B.nb[a] = (int)q;
+    }
+    B.bl = bl;
+    B.bli = 1.0 / bl;
+    B.blf = (float)bl;
+    B.blif = (float)(1.0 / bl);
+    B.cell0 = cell0;
+    B.tile0 = (int)tiles.size() / 2;
+    int starts[3][1025];
+    for (int a = 0; a < 3; ++a) {
+      // tiles of about T cells (nearest count); every tile keeps >= 2 cells
+      B.nt[a] = std::max(1, std::min(B.nb[a] / 2, (2 * B.nb[a] + T[a]) / (2 * T[a])));
+      for (int k = 0; k <= B.nt[a]; ++k) starts[a][k] = (int)((int64_t)k * B.nb[a] / B.nt[a]);
+      for (int k = 0; k < B.nt[a]; ++k)
+        if (starts[a][k + 1] - starts[a][k] + 2 > kMaxExt) {
+          delete ctx;
+          return EXAMD_ERR_ARG;
+        }
+    }
+    ctx->tile0.push_back(B.tile0);
+    for (int kz = 0; kz < B.nt[2]; ++kz)
+      for (int ky = 0; ky < B.nt[1]; ++ky)
+        for (int kx = 0; kx < B.nt[0]; ++kx) {
+          int4 d0 = make_int4(b, starts[0][kx], starts[1][ky], starts[2][kz]);
+          int4 d1 = make_int4(starts[0][kx + 1] - starts[0][kx], starts[1][ky + 1] - starts[1][ky],
+                              starts[2][kz + 1] - starts[2][kz], 0);
+          tiles.push_back(d0);
+          tiles.push_back(d1);
+          ctx->ne_max = std::max(ctx->ne_max, (d1.x + 2) * (d1.y + 2) * (d1.z + 2));
+        }
+    // boundary mask per cell: first or last cell of its tile on each axis
+    std::vector<unsigned char> edge[3];
+    for (int a = 0; a < 3; ++a) {
+      edge[a].assign(B.nb[a], 0);
+      for (int k = 0; k < B.nt[a]; ++k) {
+        edge[a][starts[a][k]] = 1;
+        edge[a][starts[a][k + 1] - 1] = 1;
+      }
+    }
+    for (int cz = 0; cz < B.nb[2]; ++cz)
+      for (int cy = 0; cy < B.nb[1]; ++cy)
+        for (int cx = 0; cx < B.nb[0]; ++cx)
+          bmask.push_back((unsigned char)(edge[0][cx] | (edge[1][cy] << 1) | (edge[2][cz] << 2)));
+    cell0 += B.nb[0] * B.nb[1] * B.nb[2];
+    ctx->atom0.push_back(a0);
+    a0 += X.natoms;
+    ctx->bh.push_back(B);
+  }
+  ctx->tile0.push_back((int)tiles.size() / 2);
+  ctx->atom0.push_back(a0);
+  ctx->N = a0;
+  ctx->NC = cell0;
+  ctx->ntiles = (int)tiles.size() / 2;
+  if (ctx->N >= (int64_t)1 << 31 || (int64_t)cell0 >= ((int64_t)1 << 31) - 1 ||
+      (cell0 + kScanTileHost - 1) / kScanTileHost > 8192 || nboxes >= (1 << 23)) {
+    delete ctx;
+    return EXAMD_ERR_ARG;
+  }
+
+  OwnLut lut;
+  if (!build_own_lut(lut)) {
+    delete ctx;
+    return EXAMD_ERR_ARG;
+  }
+  int rc = EXAMD_OK;
+#define ALLOC(ptr, cnt)                                   \
+  do {                                                    \
+    if ((rc = dalloc(ctx, &(ptr), (cnt))) != EXAMD_OK) {  \
+      free_all(ctx);                                      \
+      delete ctx;                                         \
+      return rc;                                          \
+    }                                                     \
+  } while (0)
+  if (upload_own_lut(lut) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&ctx->e0) != cudaSuccess || cudaEventCreate(&ctx->e1) != cudaSuccess ||
+      cudaEventCreate(&ctx->e2) != cudaSuccess || cudaEventCreate(&ctx->e3) != cudaSuccess) {
+    free_all(ctx);
+    delete ctx;
+    return EXAMD_ERR_CUDA;
+  }
+  const size_t N = (size_t)ctx->N, NC = (size_t)ctx->NC;
+  ALLOC(ctx->d_boxes, nboxes);
+  ALLOC(ctx->d_tiles, tiles.size());
+  ALLOC(ctx->d_tile0, nboxes + 1);
+  ALLOC(ctx->d_bmask, NC);
+  for (int b = 0; b < 2; ++b) {
+    for (int a = 0; a < 3; ++a) {
+      ALLOC(ctx->X[b][a], N);
+      ALLOC(ctx->V[b][a], N);
+    }
+    ALLOC(ctx->meta[b], N);
+    ALLOC(ctx->id[b], N);
+  }
+  ALLOC(ctx->U, N);
+  ALLOC(ctx->Uold, N);
+  ALLOC(ctx->cellS, N);
+  ALLOC(ctx->cellOld, N);
+  ALLOC(ctx->slot, N);
+  ALLOC(ctx->src, N);
+  ALLOC(ctx->count, NC);
+  ALLOC(ctx->cstart, NC + 1);
+  ALLOC(ctx->bsum, 8192);
+  ALLOC(ctx->d_total, 1);
+  if (ctx->pc.fp64) {
+    double* f;
+    ALLOC(f, 3 * N);
+    ctx->Fown = f;
+    ALLOC(f, 7 * 3 * N);
+    ctx->P = f;
+  } else {
+    float4* f;
+    ALLOC(f, N);
+    ctx->Fown = f;
+    ALLOC(f, 7 * N);
+    ctx->P = f;
+  }
+  ALLOC(ctx->tileE, ctx->ntiles);
+  ALLOC(ctx->tileW, ctx->ntiles);
+  ALLOC(ctx->tileC, 2 * (size_t)ctx->ntiles);
+  ALLOC(ctx->boxE, nboxes);
+  ALLOC(ctx->boxW, nboxes);
+  ALLOC(ctx->boxKE, nboxes);
+  ALLOC(ctx->status, 1);
+  ALLOC(ctx->d_occ, 2);
+  ALLOC(ctx->stage, 3 * N);
+  ALLOC(ctx->stage2, 3 * N);
+  ALLOC(ctx->d_meta_in, N);
+  ALLOC(ctx->d_factor, nboxes);
+#undef ALLOC
+  cudaStream_t st = ctx->st;
+  bool ok = cudaMemcpyAsync(ctx->d_boxes, ctx->bh.data(), nboxes * sizeof(BoxDev), cudaMemcpyHostToDevice, st) ==
+                cudaSuccess &&
+            cudaMemcpyAsync(ctx->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, st) ==
+                cudaSuccess &&
+            cudaMemcpyAsync(ctx->d_tile0, ctx->tile0.data(), (nboxes + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                            st) == cudaSuccess &&
+            cudaMemcpyAsync(ctx->d_bmask, bmask.data(), NC, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemsetAsync(ctx->count, 0, NC * sizeof(int), st) == cudaSuccess &&
+            cudaMemsetAsync(ctx->status, 0, sizeof(int), st) == cudaSuccess &&
+            cudaStreamSynchronize(st) == cudaSuccess;
+  if (!ok) {
+    free_all(ctx);
+    delete ctx;
+    return EXAMD_ERR_CUDA;
+  }
+  *out = ctx;
+  return EXAMD_OK;
+}
+
+void examd_gpu_destroy(examd_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->dev);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  free_all(ctx);
+  delete ctx;
+}
+
+}  // extern "C"
+
+// --------------------------------------------------------------------------
+namespace {
+
+inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
+
+// Scan, place and final ordering after a counting pass; swaps the buffers.
+int finish_binning(examd_ctx* ctx) {
+  cudaStream_t st = ctx->st;
+  const int nc = ctx->NC;
+  const int nsb = (nc + kScanTileHost - 1) / kScanTileHost;
+  const int s = ctx->cur, d = 1 - ctx->cur;
+  k_scan_reduce<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum);
+  k_scan_top<<<1, 1024, 0, st>>>(nsb, ctx->bsum, ctx->d_total);
+  k_scan_final<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum, ctx->cstart);
+  if (ctx->N > 0) {
+    k_place<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, nc, ctx->cellOld, ctx->slot, ctx->cstart, ctx->src);
+    k_finalize<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, ctx->src, ctx->cellOld, ctx->cstart, ctx->Uold,
+                                              ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->V[s][0],
+                                              ctx->V[s][1], ctx->V[s][2], ctx->meta[s], ctx->id[s],
+                                              ctx->X[d][0], ctx->X[d][1], ctx->X[d][2], ctx->V[d][0],
+                                              ctx->V[d][1], ctx->V[d][2], ctx->meta[d], ctx->id[d], ctx->U,
+                                              ctx->cellS);
+  } else {
+    k_place<<<1, 32, 0, st>>>(0, nc, ctx->cellOld, ctx->slot, ctx->cstart, ctx->src);
+  }
+  CK(cudaGetLastError());
+  ctx->cur = d;
+  return EXAMD_OK;
+}
+
+int check_status(examd_ctx* ctx) {
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (h) {
+    CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  return status_to_code(h);
+}
+
+// Staged-atom capacity of a tile from the current binning (+25% + 64 headroom).
+int update_capacity(examd_ctx* ctx) {
+  CK(cudaMemsetAsync(ctx->d_occ, 0, 2 * sizeof(int), ctx->st));
+  k_tile_occupancy<<<ctx->ntiles, 128, 0, ctx->st>>>(ctx->d_tiles, ctx->d_boxes, ctx->cstart, ctx->d_occ);
+  CK(cudaGetLastError());
+  int occ = 0;
+  CK(cudaMemcpyAsync(&occ, ctx->d_occ, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  int want = ((occ + occ / 4 + 64) + 31) & ~31;
+  if (want <= ctx->cap) return EXAMD_OK;
+  int bytes = pair_smem_bytes(ctx->pc, want, ctx->ne_max);
+  if (bytes > ctx->smem_limit) {
+    // fall back to the exact need if the headroom does not fit
+    want = (occ + 31) & ~31;
+    bytes = pair_smem_bytes(ctx->pc, want, ctx->ne_max);
+    if (bytes > ctx->smem_limit) return EXAMD_ERR_CELL_OVERFLOW;
+  }
+  ctx->cap = want;
+  ctx->smem = bytes;
+  // all variants used by this context
+  PairConfig c = ctx->pc;
+  for (int e = 0; e < 2; ++e)
+    for (int n = 0; n < 2; ++n) {
+      c.energy = e;
+      c.count = n;
+      CK(pair_prepare(c, bytes));
+    }
+  return EXAMD_OK;
+}
+
+PairArgs pair_args(examd_ctx* ctx) {
+  PairArgs a{};
+  a.tiles = ctx->d_tiles;
+  a.boxes = ctx->d_boxes;
+  a.cstart = ctx->cstart;
+  a.U = ctx->U;
+  a.X0 = ctx->X[ctx->cur][0];
+  a.X1 = ctx->X[ctx->cur][1];
+  a.X2 = ctx->X[ctx->cur][2];
+  a.Fown = ctx->Fown;
+  a.P = ctx->P;
+  a.N = ctx->N;
+  a.tileE = ctx->tileE;
+  a.tileW = ctx->tileW;
+  a.tileC = ctx->tileC;
+  a.status = ctx->status;
+  a.cap = ctx->cap;
+  a.ne_max = ctx->ne_max;
+  a.lj = ctx->lj;
+  return a;
+}
+
+int run_pair(examd_ctx* ctx, bool energy, bool count, double* boxE = nullptr, double* boxW = nullptr) {
+  PairConfig c = ctx->pc;
+  c.energy = energy;
+  c.count = count;
+  CK(launch_pair(c, pair_args(ctx), ctx->ntiles, ctx->smem, ctx->st));
+  if (energy)
+    CK(launch_reduce_tiles(ctx->nboxes, ctx->d_tile0, ctx->tileE, ctx->tileW, boxE ? boxE : ctx->boxE,
+                           boxW ? boxW : ctx->boxW, ctx->st));
+  return EXAMD_OK;
+}
+
+StepArgs step_args(examd_ctx* ctx) {
+  StepArgs s{};
+  s.boxes = ctx->d_boxes;
+  s.bmask = ctx->d_bmask;
+  s.cellS = ctx->cellS;
+  s.Fown = ctx->Fown;
+  s.P = ctx->P;
+  s.N = ctx->N;
+  s.fp64 = ctx->pc.fp64;
+  return s;
+}
+
+int forces_common(examd_ctx* ctx, double* forces, double* epot, double* virial, int accumulate) {
+  cudaStream_t st = ctx->st;
+  const bool energy = epot || virial;
+  int rc = run_pair(ctx, energy, false);
+  if (rc) return rc;
+  if (forces) {
+    if (accumulate) CK(cudaMemcpyAsync(ctx->stage, forces, 3 * ctx->N * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(launch_forces_out(step_args(ctx), ctx->id[ctx->cur], ctx->stage, accumulate, st));
+    CK(cudaMemcpyAsync(forces, ctx->stage, 3 * ctx->N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  if (epot) CK(cudaMemcpyAsync(epot, ctx->boxE, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (virial) CK(cudaMemcpyAsync(virial, ctx->boxW, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  rc = check_status(ctx);
+  if (rc) return rc;
+  ctx->forces_valid = true;
+  return EXAMD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int examd_gpu_set_atoms(examd_ctx* ctx, int64_t n, const double* pos, const int* type, const double* vel) {
+  if (!ctx || (n > 0 && !pos) || n != ctx->N) return EXAMD_ERR_ARG;
+  cudaSetDevice(ctx->dev);
+  cudaStream_t st = ctx->st;
+  std::vector<int> meta((size_t)n);
+  for (int b = 0; b < ctx->nboxes; ++b)
+    for (int64_t i = ctx->atom0[b]; i < ctx->atom0[b + 1]; ++i) {
+      int t = type ? type[i] : 0;
+      if (t < 0 || t >= ctx->p.ntypes) return EXAMD_ERR_ARG;
+      meta[(size_t)i] = (b << 8) | t;
+    }
+  if (n > 0) {
+    CK(cudaMemcpyAsync(ctx->stage, pos, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (vel) CK(cudaMemcpyAsync(ctx->stage2, vel, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->d_meta_in, meta.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), st));
+  const int s = ctx->cur;
+  if (n > 0) {
+    k_load_bin<<<nblk(n), 256, 0, st>>>(n, ctx->stage, vel ? ctx->stage2 : nullptr, ctx->d_meta_in, ctx->d_boxes,
+                                        ctx->p.strict_box, ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->V[s][0],
+                                        ctx->V[s][1], ctx->V[s][2], ctx->meta[s], ctx->id[s], ctx->cellOld,
+                                        ctx->slot, ctx->Uold, ctx->count, ctx->status);
+    CK(cudaGetLastError());
+  }
+  int rc = finish_binning(ctx);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(st));
+  rc = check_status(ctx);
+  if (rc) return rc;
+  rc = update_capacity(ctx);
+  if (rc) return rc;
+  ctx->atoms_set = true;
+  ctx->forces_valid = false;
+  return EXAMD_OK;
+}
+
+int examd_gpu_forces(examd_ctx* ctx, double* forces, double* epot, double* virial, int accumulate) {
+  if (!ctx) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  return forces_common(ctx, forces, epot, virial, accumulate);
+}
+
+int examd_gpu_forces_at(examd_ctx* ctx, const double* pos, double* forces, double* epot, double* virial,
+                        int accumulate) {
+  if (!ctx || (ctx->N > 0 && !pos)) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  cudaStream_t st = ctx->st;
+  const int s = ctx->cur;
+  if (ctx->N > 0) {
+    CK(cudaMemcpyAsync(ctx->stage2, pos, 3 * ctx->N * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_gather_pos_bin<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, ctx->stage2, ctx->d_boxes, ctx->p.strict_box,
+                                                   ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->meta[s],
+                                                   ctx->id[s], ctx->cellOld, ctx->slot, ctx->Uold, ctx->count,
+                                                   ctx->status);
+    CK(cudaGetLastError());
+  }
+  int rc = finish_binning(ctx);
+  if (rc) return rc;
+  return forces_common(ctx, forces, epot, virial, accumulate);
+}
+
+}  // extern "C"
+
+namespace {
+
+KickArgs kick_args(examd_ctx* ctx, double ckick, double dt, bool drift, double hk, double* boxKE) {
+  KickArgs k{};
+  k.s = step_args(ctx);
+  const int c = ctx->cur;
+  for (int a = 0; a < 3; ++a) {
+    k.X[a] = ctx->X[c][a];
+    k.V[a] = ctx->V[c][a];
+  }
+  k.meta = ctx->meta[c];
+  k.ckick = ckick;
+  k.dt = dt;
+  k.drift = drift;
+  k.hk = hk;
+  k.boxKE = boxKE;
+  k.lj = ctx->lj;
+  k.cellOld = ctx->cellOld;
+  k.slot = ctx->slot;
+  k.Uold = ctx->Uold;
+  k.count = ctx->count;
+  k.status = ctx->status;
+  return k;
+}
+
+// One step after the first: kick(ck) + drift + bin, pair.  keSlot receives the
+// kinetic energy at the start of this step, eSlot the potential energy after.
+int step_once(examd_ctx* ctx, double ck, double dt, double* keSlot, double* eSlot, double* wSlot) {
+  const double h = 0.5 * dt;
+  CK(launch_kick(kick_args(ctx, ck, dt, true, keSlot ? h : 0.0, keSlot), ctx->st));
+  int rc = finish_binning(ctx);
+  if (rc) return rc;
+  return run_pair(ctx, eSlot != nullptr, false, eSlot, wSlot);
+}
+
+int ensure_ebuf(examd_ctx* ctx, int steps) {
+  if (steps <= ctx->ebuf_steps) return EXAMD_OK;
+  if (ctx->boxE) cudaFree(ctx->boxE);
+  if (ctx->boxW) cudaFree(ctx->boxW);
+  if (ctx->boxKE) cudaFree(ctx->boxKE);
+  ctx->boxE = ctx->boxW = ctx->boxKE = nullptr;
+  size_t n = (size_t)(steps + 1) * ctx->nboxes;
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->boxE, n)) || (rc = dalloc(ctx, &ctx->boxW, n)) || (rc = dalloc(ctx, &ctx->boxKE, n)))
+    return rc;
+  ctx->ebuf_steps = steps;
+  if (ctx->gexec) {
+    cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+  }
+  return EXAMD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int examd_gpu_run(examd_ctx* ctx, int nsteps, double dt, int graph_chunk, double* energies, examd_stats* stats) {
+  if (!ctx || nsteps < 0 || !(dt > 0) || graph_chunk < 0) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  cudaStream_t st = ctx->st;
+  const int nb = ctx->nboxes;
+  const bool wantE = energies != nullptr;
+  int chunk = graph_chunk > 0 ? (graph_chunk + 1) / 2 * 2 : 0;
+  int rc = ensure_ebuf(ctx, std::max(chunk, 1) + 1);
+  if (rc) return rc;
+  if (!ctx->forces_valid) {
+    rc = run_pair(ctx, false, false);
+    if (rc) return rc;
+    ctx->forces_valid = true;
+  }
+  if (nsteps == 0) return EXAMD_OK;
+  const double h = 0.5 * dt;
+  CK(cudaEventRecord(ctx->e0, st));
+  // step 1: half kick + drift, then forces
+  if (wantE) CK(cudaMemsetAsync(ctx->boxKE, 0, (size_t)(ctx->ebuf_steps + 1) * nb * sizeof(double), st));
+  rc = step_once(ctx, h, dt, nullptr, wantE ? ctx->boxE : nullptr, wantE ? ctx->boxW : nullptr);
+  if (rc) return rc;
+  if (wantE) {
+    // energies[0] epot now; ekin later
+    for (int b = 0; b < nb; ++b)
+      CK(cudaMemcpyAsync(&energies[2 * b + 1], ctx->boxE + b, sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  int done = 1;
+  // steady state: merged kicks v += dt F/m
+  while (done < nsteps) {
+    const int left = nsteps - done;
+    if (chunk > 0 && left >= chunk) {
+      const bool rebuild = !ctx->gexec || ctx->g_parity != ctx->cur || ctx->g_chunk != chunk ||
+                           ctx->g_energy != (int)wantE || ctx->g_dt != dt || ctx->g_cap != ctx->cap;
+      if (rebuild) {
+        if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+        const int parity = ctx->cur;
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        if (wantE) cudaMemsetAsync(ctx->boxKE, 0, (size_t)(chunk + 1) * nb * sizeof(double), st);
+        int src = EXAMD_OK;
+        for (int j = 0; j < chunk && src == EXAMD_OK; ++j)
+          src = step_once(ctx, dt, dt, wantE ? ctx->boxKE + (size_t)j * nb : nullptr,
+                          wantE ? ctx->boxE + (size_t)j * nb : nullptr, wantE ? ctx->boxW + (size_t)j * nb : nullptr);
+        cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (src != EXAMD_OK) return src;
+        if (ce != cudaSuccess) return ctx->cuda_fail(ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&ctx->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return ctx->cuda_fail(ce, "cudaGraphInstantiate");
+        // capture advanced the host-side parity; the graph leaves it unchanged (chunk even)
+        ctx->cur = parity;
+        ctx->g_parity = parity;
+        ctx->g_chunk = chunk;
+        ctx->g_energy = wantE;
+        ctx->g_dt = dt;
+        ctx->g_cap = ctx->cap;
+      }
+      CK(cudaGraphLaunch(ctx->gexec, st));
+      if (wantE) {
+        // slot j: ekin at the start of local step j (= after global step done + j), epot after it
+        for (int j = 0; j < chunk; ++j)
+          for (int b = 0; b < nb; ++b) {
+            const size_t gs = (size_t)(done + j);  // global 0-based step index of epot
+            CK(cudaMemcpyAsync(&energies[2 * ((gs - 1) * nb + b)], ctx->boxKE + (size_t)j * nb + b,
+                               sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(&energies[2 * (gs * nb + b) + 1], ctx->boxE + (size_t)j * nb + b, sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+          }
+        CK(cudaStreamSynchronize(st));  // buffers are reused by the next replay
+      }
+      done += chunk;
+      // the capacity may need to grow as the density fluctuates
+      CK(cudaStreamSynchronize(st));
+      rc = check_status(ctx);
+      if (rc) return rc;
+      rc = update_capacity(ctx);
+      if (rc) return rc;
+    } else {
+      double* ke = nullptr;
+      if (wantE) {
+        CK(cudaMemsetAsync(ctx->boxKE, 0, nb * sizeof(double), st));
+        ke = ctx->boxKE;
+      }
+      rc = step_once(ctx, dt, dt, ke, wantE ? ctx->boxE : nullptr, wantE ? ctx->boxW : nullptr);
+      if (rc) return rc;
+      if (wantE)
+        for (int b = 0; b < nb; ++b) {
+          CK(cudaMemcpyAsync(&energies[2 * ((size_t)(done - 1) * nb + b)], ctx->boxKE + b, sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+          CK(cudaMemcpyAsync(&energies[2 * ((size_t)done * nb + b) + 1], ctx->boxE + b, sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+        }
+      if (wantE) CK(cudaStreamSynchronize(st));
+      done += 1;
+    }
+  }
+  // closing half kick: v(t_n) = v(t_n - h) + h F/m
+  if (wantE) CK(cudaMemsetAsync(ctx->boxKE, 0, nb * sizeof(double), st));
+  CK(launch_kick(kick_args(ctx, h, dt, false, wantE ? h : 0.0, ctx->boxKE), st));
+  if (wantE)
+    for (int b = 0; b < nb; ++b)
+      CK(cudaMemcpyAsync(&energies[2 * ((size_t)(nsteps - 1) * nb + b)], ctx->boxKE + b, sizeof(double),
+                         cudaMemcpyDeviceToHost, st));
+  CK(cudaEventRecord(ctx->e1, st));
+  CK(cudaStreamSynchronize(st));
+  rc = check_status(ctx);
+  if (rc) return rc;
+  ctx->forces_valid = true;
+  if (stats) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->e0, ctx->e1));
+    std::memset(stats, 0, sizeof(*stats));
+    stats->ms = ms;
+    stats->steps = nsteps;
+    if (wantE) {
+      for (int b = 0; b < nb; ++b) {
+        stats->ekin += energies[2 * ((size_t)(nsteps - 1) * nb + b)];
+        stats->epot += energies[2 * ((size_t)(nsteps - 1) * nb + b) + 1];
+      }
+    }
+  }
+  return EXAMD_OK;
+}
+
+int examd_gpu_get_state(examd_ctx* ctx, double* pos, double* vel) {
+  if (!ctx) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  const int c = ctx->cur;
+  if (pos) {
+    CK(launch_state_out(ctx->N, ctx->X[c], ctx->id[c], ctx->stage, ctx->st));
+    CK(cudaMemcpyAsync(pos, ctx->stage, 3 * ctx->N * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  }
+  if (vel) {
+    CK(launch_state_out(ctx->N, ctx->V[c], ctx->id[c], ctx->stage2, ctx->st));
+    CK(cudaMemcpyAsync(vel, ctx->stage2, 3 * ctx->N * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  }
+  CK(cudaStreamSynchronize(ctx->st));
+  return EXAMD_OK;
+}
+
+int examd_gpu_kinetic(examd_ctx* ctx, double* ekin) {
+  if (!ctx || !ekin) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  const int c = ctx->cur;
+  CK(cudaMemsetAsync(ctx->boxKE, 0, ctx->nboxes * sizeof(double), ctx->st));
+  CK(launch_kinetic(ctx->N, ctx->V[c], ctx->meta[c], ctx->lj, ctx->boxKE, ctx->st));
+  CK(cudaMemcpyAsync(ekin, ctx->boxKE, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return EXAMD_OK;
+}
+
+int examd_gpu_scale_velocities(examd_ctx* ctx, const double* factor) {
+  if (!ctx || !factor) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  const int c = ctx->cur;
+  CK(cudaMemcpyAsync(ctx->d_factor, factor, ctx->nboxes * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  CK(launch_scale_v(ctx->N, ctx->V[c], ctx->meta[c], ctx->d_factor, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return EXAMD_OK;
+}
+
+int examd_gpu_time_forces(examd_ctx* ctx, int reps, double* ms, double* kernel_ms) {
+  if (!ctx || reps < 1) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  cudaStream_t st = ctx->st;
+  int rc = run_pair(ctx, false, false);  // warm-up
+  if (rc) return rc;
+  CK(cudaEventRecord(ctx->e0, st));
+  for (int r = 0; r < reps; ++r) {
+    rc = run_pair(ctx, false, false);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(ctx->e1, st));
+  CK(cudaStreamSynchronize(st));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, ctx->e0, ctx->e1));
+  if (ms) *ms = t;
+  if (kernel_ms) *kernel_ms = t / reps;
+  rc = check_status(ctx);
+  if (rc) return rc;
+  ctx->forces_valid = true;
+  return EXAMD_OK;
+}
+
+int examd_gpu_counters(examd_ctx* ctx, int64_t* candidates, int64_t* accepted, int64_t* tiles,
+                       int64_t* max_tile_atoms) {
+  if (!ctx) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  int rc = run_pair(ctx, false, true);
+  if (rc) return rc;
+  std::vector<long long> c(2 * (size_t)ctx->ntiles);
+  CK(cudaMemcpyAsync(c.data(), ctx->tileC, c.size() * sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
+  int occ = 0;
+  CK(cudaMemsetAsync(ctx->d_occ, 0, 2 * sizeof(int), ctx->st));
+  k_tile_occupancy<<<ctx->ntiles, 128, 0, ctx->st>>>(ctx->d_tiles, ctx->d_boxes, ctx->cstart, ctx->d_occ);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&occ, ctx->d_occ, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  rc = check_status(ctx);
+  if (rc) return rc;
+  long long s1 = 0, s2 = 0;
+  for (int t = 0; t < ctx->ntiles; ++t) {
+    s1 += c[2 * t];
+    s2 += c[2 * t + 1];
+  }
+  if (candidates) *candidates = s1;
+  if (accepted) *accepted = s2;
+  if (tiles) *tiles = ctx->ntiles;
+  if (max_tile_atoms) *max_tile_atoms = occ;
+  ctx->forces_valid = true;
+  return EXAMD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,257 @@
+// bin.cu -- cell binning: a counting sort of the atoms into the reference's
+// block grid, rebuilt on every step.
+//
+// Replaces exaMD_identify_block (SRC/exaMD_module.f90:101-125) and the
+// per-block linked lists built once by exaMD_particles_generate /
+// exaMD_read_particles (SRC/exaMD_input_formats.f90:66-92, 169-192).  The
+// result is the reference's own block order: cells in (z, y, x) order, atoms of
+// a cell in ascending caller index.  HBM-bound work.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace examd {
+
+// Cell of one coordinate and the offset from the cell origin c * bl.  bl has at
+// most 13 significant bits, so c * bl is exact in FP32 and x - c * bl is exact
+// in FP64: the cell is exactly Int(x / bl) of the exact quotient, with the
+// last cell absorbing the remainder (SRC/exaMD_module.f90:109-113).
+__device__ __forceinline__ int cell_of(double x, float blf, float blif, int nb, float& u) {
+  float xh = (float)x;
+  int c = (int)(xh * blif);
+  c = min(max(c, 0), nb - 1);
+  double ud = x - (double)((float)c * blf);
+  if (ud < 0.0) {  // FP32 estimate one too high
+    c = max(c - 1, 0);
+    ud = x - (double)((float)c * blf);
+  } else if (c < nb - 1 && (float)ud >= blf) {  // possibly one too low
+    if (ud >= (double)blf) {
+      c += 1;
+      ud = x - (double)((float)c * blf);
+    }
+  }
+  u = (float)ud;
+  return c;
+}
+
+__device__ __forceinline__ void bin_one(int s, double x, double y, double z, int meta,
+                                        const BoxDev* __restrict__ boxes, int* __restrict__ cellOld,
+                                        int* __restrict__ slot, float4* __restrict__ Uold,
+                                        int* __restrict__ count, int* __restrict__ status) {
+  const BoxDev& B = boxes[meta >> 8];
+  if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+    atomicOr(status, ST_NONFINITE);
+    x = y = z = 0.0;
+  }
+  float ux, uy, uz;
+  int cx = cell_of(x, B.blf, B.blif, B.nb[0], ux);
+  int cy = cell_of(y, B.blf, B.blif, B.nb[1], uy);
+  int cz = cell_of(z, B.blf, B.blif, B.nb[2], uz);
+  int gc = B.cell0 + cx + B.nb[0] * (cy + B.nb[1] * cz);
+  cellOld[s] = gc;
+  Uold[s] = make_float4(ux, uy, uz, __int_as_float(meta & 0xff));
+  slot[s] = atomicAdd(&count[gc], 1);
+}
+
+// Load caller-order AoS positions (and velocities) into the SoA master arrays,
+// wrapping (or, in strict mode, rejecting) positions outside [0, L), and bin.
+__global__ void k_load_bin(int64_t n, const double* __restrict__ aos, const double* __restrict__ vaos,
+                           const int* __restrict__ meta_in, const BoxDev* __restrict__ boxes, int strict,
+                           double* __restrict__ X0, double* __restrict__ X1, double* __restrict__ X2,
+                           double* __restrict__ V0, double* __restrict__ V1, double* __restrict__ V2,
+                           int* __restrict__ meta, int* __restrict__ id, int* __restrict__ cellOld,
+                           int* __restrict__ slot, float4* __restrict__ Uold, int* __restrict__ count,
+                           int* __restrict__ status) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int mt = meta_in[s];
+  const BoxDev& B = boxes[mt >> 8];
+  double p[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double x = aos[3 * s + a];
+    if (strict && !(x >= 0.0 && x < B.L[a])) atomicOr(status, ST_OUTSIDE);
+    p[a] = isfinite(x) ? wrap_coord(x, B.L[a], B.Li[a], B.Lf[a]) : x;
+  }
+  X0[s] = p[0];
+  X1[s] = p[1];
+  X2[s] = p[2];
+  if (vaos) {
+    V0[s] = vaos[3 * s];
+    V1[s] = vaos[3 * s + 1];
+    V2[s] = vaos[3 * s + 2];
+  } else {
+    V0[s] = V1[s] = V2[s] = 0.0;
+  }
+  meta[s] = mt;
+  id[s] = (int)s;
+  bin_one((int)s, p[0], p[1], p[2], mt, boxes, cellOld, slot, Uold, count, status);
+}
+
+// New positions in caller order (AoS) for atoms already held in sorted order:
+// gather by id, wrap, bin.
+__global__ void k_gather_pos_bin(int64_t n, const double* __restrict__ aos, const BoxDev* __restrict__ boxes,
+                                 int strict, double* __restrict__ X0, double* __restrict__ X1,
+                                 double* __restrict__ X2, const int* __restrict__ meta,
+                                 const int* __restrict__ id, int* __restrict__ cellOld, int* __restrict__ slot,
+                                 float4* __restrict__ Uold, int* __restrict__ count, int* __restrict__ status) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int mt = meta[s];
+  const BoxDev& B = boxes[mt >> 8];
+  int64_t i = id[s];
+  double p[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double x = aos[3 * i + a];
+    if (strict && !(x >= 0.0 && x < B.L[a])) atomicOr(status, ST_OUTSIDE);
+    p[a] = isfinite(x) ? wrap_coord(x, B.L[a], B.Li[a], B.Lf[a]) : x;
+  }
+  X0[s] = p[0];
+  X1[s] = p[1];
+  X2[s] = p[2];
+  bin_one((int)s, p[0], p[1], p[2], mt, boxes, cellOld, slot, Uold, count, status);
+}
+
+// Bin the current positions without moving them (after a velocity-only change
+// or to rebuild the cell lists).
+__global__ void k_bin(int64_t n, const double* __restrict__ X0, const double* __restrict__ X1,
+                      const double* __restrict__ X2, const int* __restrict__ meta,
+                      const BoxDev* __restrict__ boxes, int* __restrict__ cellOld, int* __restrict__ slot,
+                      float4* __restrict__ Uold, int* __restrict__ count, int* __restrict__ status) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  bin_one((int)s, X0[s], X1[s], X2[s], meta[s], boxes, cellOld, slot, Uold, count, status);
+}
+
+// ---- exclusive scan of the cell counts (three passes) ----------------------
+constexpr int kScanThreads = 256, kScanItems = 8, kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* sh, int& total) {
+  // sh: kScanThreads/32 ints
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int nw = blockDim.x >> 5;
+    int t = lane < nw ? sh[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < nw) sh[lane] = t;
+  }
+  __syncthreads();
+  int base = w > 0 ? sh[w - 1] : 0;
+  total = sh[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return base + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(int nc, const int* __restrict__ count,
+                                                              int* __restrict__ bsum) {
+  __shared__ int sh[kScanThreads / 32];
+  int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) s += (base + k < nc) ? count[base + k] : 0;
+  int total;
+  block_exclusive_scan(s, sh, total);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// One block scans up to kScanTile * 4 block sums.
+__global__ void __launch_bounds__(1024) k_scan_top(int nb, int* __restrict__ bsum, int* __restrict__ total_out) {
+  __shared__ int sh[32];
+  constexpr int kItems = 8;
+  int base = threadIdx.x * kItems;
+  int v[kItems], s = 0;
+#pragma unroll
+  for (int k = 0; k < kItems; ++k) {
+    v[k] = (base + k < nb) ? bsum[base + k] : 0;
+    s += v[k];
+  }
+  int total;
+  int ex = block_exclusive_scan(s, sh, total);
+#pragma unroll
+  for (int k = 0; k < kItems; ++k) {
+    if (base + k < nb) bsum[base + k] = ex;
+    ex += v[k];
+  }
+  if (threadIdx.x == 0) *total_out = total;
+}
+
+// Final pass: cstart = exclusive scan; counts are zeroed for the next binning.
+// cstart[nc] (the atom count) is written by k_place.
+__global__ void __launch_bounds__(kScanThreads) k_scan_final(int nc, int* __restrict__ count,
+                                                             const int* __restrict__ bsum,
+                                                             int* __restrict__ cstart) {
+  __shared__ int sh[kScanThreads / 32];
+  int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int v[kScanItems], s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = (base + k < nc) ? count[base + k] : 0;
+    s += v[k];
+  }
+  int total;
+  int ex = block_exclusive_scan(s, sh, total) + bsum[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < nc) {
+      cstart[base + k] = ex;
+      count[base + k] = 0;
+    }
+    ex += v[k];
+  }
+}
+
+// Slot of every atom inside its cell (arbitrary order from the atomics).
+__global__ void k_place(int64_t n, int nc, const int* __restrict__ cellOld, const int* __restrict__ slot,
+                        int* __restrict__ cstart, int* __restrict__ src) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s == 0) cstart[nc] = (int)n;
+  if (s >= n) return;
+  src[cstart[cellOld[s]] + slot[s]] = (int)s;
+}
+
+// Final order: inside each cell the atoms are ranked by caller index (the
+// reference's linked-list order), then every per-atom array is gathered into
+// the other buffer.
+__global__ void k_finalize(int64_t n, const int* __restrict__ src, const int* __restrict__ cellOld,
+                           const int* __restrict__ cstart, const float4* __restrict__ Uold,
+                           const double* __restrict__ X0, const double* __restrict__ X1,
+                           const double* __restrict__ X2, const double* __restrict__ V0,
+                           const double* __restrict__ V1, const double* __restrict__ V2,
+                           const int* __restrict__ meta, const int* __restrict__ id, double* __restrict__ Y0,
+                           double* __restrict__ Y1, double* __restrict__ Y2, double* __restrict__ W0,
+                           double* __restrict__ W1, double* __restrict__ W2, int* __restrict__ meta2,
+                           int* __restrict__ id2, float4* __restrict__ U, int* __restrict__ cellS) {
+  int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  int s = src[j];
+  int c = cellOld[s];
+  int st = cstart[c], en = cstart[c + 1];
+  int myid = id[s];
+  int rank = 0;
+  for (int k = st; k < en; ++k) rank += (id[src[k]] < myid);
+  int d = st + rank;
+  Y0[d] = X0[s];
+  Y1[d] = X1[s];
+  Y2[d] = X2[s];
+  W0[d] = V0[s];
+  W1[d] = V1[s];
+  W2[d] = V2[s];
+  meta2[d] = meta[s];
+  id2[d] = myid;
+  U[d] = Uold[s];
+  cellS[d] = c;
+}
+
+}  // namespace examd

@@ -1,0 +1,125 @@
+// common.cuh -- shared device-side definitions of the GB300 midpoint LJ path.
+//
+// Layout in HBM (all per-atom arrays in "sorted order": atoms grouped by cell,
+// cells in (box, z, y, x) order, atoms of a cell in ascending caller index,
+// i.e. the reference's block order and linked-list order,
+// SRC/exaMD_input_formats.f90:66-92):
+//   X[3][N], V[3][N]  FP64 positions / velocities (SoA), double-buffered
+//   meta[N]           box << 8 | type
+//   id[N]             caller index
+//   U[N]              float4 (u_x, u_y, u_z, type bits): position relative to
+//                     the atom's cell origin c * block_length, FP32
+//   cellS[N]          global cell id
+//   cstart[NC+1]      CSR offsets of cells
+//   Fown[N], P[7][N]  force partials: the owning tile's sum, and the sums of
+//                     up to 7 neighbouring tiles whose halo holds the atom
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/examd_gb300.h"
+
+namespace examd {
+
+constexpr int kRows = 13;     // 12 full x-rows of 5 cells + the half self row
+constexpr int kClasses = 125; // 5 position classes per axis inside a tile
+constexpr int kMaxExt = 31;   // ext-cell coordinate packing: 5 bits per axis
+
+// Status word bits (device -> host).
+enum StatusBits : int {
+  ST_OVERFLOW = 1,   // a tile has more staged atoms than the smem capacity
+  ST_NONFINITE = 2,  // NaN / Inf position
+  ST_OUTSIDE = 4,    // position outside [0,L) in strict mode
+  ST_TIMEOUT = 8,    // a bounded wait gave up
+};
+
+struct BoxDev {
+  double L[3], Li[3];
+  double bl, bli;  // block_length (cell edge) and its inverse
+  float blf, blif, Lf[3];
+  int nb[3];
+  int cell0;       // first global cell id of the box
+  int tile0;       // first tile of the box
+  int nt[3];       // tiles per axis
+};
+
+// LJ parameters per ordered type pair, FP32 (mixed) and FP64.
+struct LJ32 {
+  float sig2, m24eps, c4eps, rc2;  // m24eps = -24 eps (dg prefactor)
+};
+struct LJ64 {
+  double sig2, eps24, eps4, rc2;   // as user_func.f90:58-59 computes them
+};
+
+struct LJTable {
+  int nt;
+  float rc2max;
+  LJ32 p32[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];
+  LJ64 p64[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];
+  double minv[EXAMD_MAX_TYPES];
+  double mass[EXAMD_MAX_TYPES];
+};
+
+// Ownership masks of the midpoint table, filled once per process.
+//   c_rows[r] = (dy, dz) of row r (r = 12: the self row (0,0))
+//   c_lut[cls][r] = 5-bit mask over dx = -2..2 of the cell pairs (A, A+d)
+//   owned by the tile when A's position class is cls.  Row 12 uses bit 2 for
+//   the pairs inside A (a1 < a2) and bits 3, 4 for dx = +1, +2.
+struct OwnLut {
+  signed char rows[kRows][2];
+  unsigned char lut[kClasses][kRows];
+};
+
+__host__ __device__ inline int pos_class(int l, int t) {
+  return l < 0 ? 0 : (l == 0 ? 1 : (l < t - 1 ? 2 : (l == t - 1 ? 3 : 4)));
+}
+
+// Tile descriptor: int4 {box, x0, y0, z0}, int4 {tx, ty, tz, 0}.
+
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ int warp_min(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Kahan-compensated FP32 accumulator.
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+
+// Periodic wrap of an FP64 coordinate into [0, L); the common in-range case
+// is decided in FP32 (FP64 instructions are scarce on this part).
+__device__ __forceinline__ double wrap_coord(double x, double L, double Li, float Lf) {
+  float xf = (float)x;
+  if (xf > 1e-3f && xf < Lf - 1e-3f) return x;
+  double y = x - floor(x * Li) * L;
+  if (y >= L) y -= L;
+  if (y < 0.0) y += L;
+  return y;
+}
+
+}  // namespace examd

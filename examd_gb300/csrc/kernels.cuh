@@ -1,0 +1,107 @@
+// kernels.cuh -- host-side launchers of the device kernels (one per .cu file).
+#pragma once
+
+#include "common.cuh"
+
+namespace examd {
+
+// ---- bin.cu -----------------------------------------------------------------
+__global__ void k_load_bin(int64_t n, const double* aos, const double* vaos, const int* meta_in,
+                           const BoxDev* boxes, int strict, double* X0, double* X1, double* X2, double* V0,
+                           double* V1, double* V2, int* meta, int* id, int* cellOld, int* slot, float4* Uold,
+                           int* count, int* status);
+__global__ void k_gather_pos_bin(int64_t n, const double* aos, const BoxDev* boxes, int strict, double* X0,
+                                 double* X1, double* X2, const int* meta, const int* id, int* cellOld, int* slot,
+                                 float4* Uold, int* count, int* status);
+__global__ void k_bin(int64_t n, const double* X0, const double* X1, const double* X2, const int* meta,
+                      const BoxDev* boxes, int* cellOld, int* slot, float4* Uold, int* count, int* status);
+__global__ void k_scan_reduce(int nc, const int* count, int* bsum);
+__global__ void k_scan_top(int nb, int* bsum, int* total_out);
+__global__ void k_scan_final(int nc, int* count, const int* bsum, int* cstart);
+__global__ void k_place(int64_t n, int nc, const int* cellOld, const int* slot, int* cstart, int* src);
+__global__ void k_finalize(int64_t n, const int* src, const int* cellOld, const int* cstart, const float4* Uold,
+                           const double* X0, const double* X1, const double* X2, const double* V0,
+                           const double* V1, const double* V2, const int* meta, const int* id, double* Y0,
+                           double* Y1, double* Y2, double* W0, double* W1, double* W2, int* meta2, int* id2,
+                           float4* U, int* cellS);
+constexpr int kScanTileHost = 2048;  // cells per scan block (kScanThreads * kScanItems)
+
+// ---- pair.cu ----------------------------------------------------------------
+struct PairArgs {
+  const int4* tiles;  // 2 int4 per tile
+  const BoxDev* boxes;
+  const int* cstart;
+  const float4* U;
+  const double* X0;
+  const double* X1;
+  const double* X2;
+  void* Fown;  // mixed: float4[N]; fp64: double[3][N]
+  void* P;     // mixed: float4[7][N]; fp64: double[7][3][N]
+  int64_t N;
+  double* tileE;     // per tile potential energy
+  double* tileW;     // per tile virial
+  long long* tileC;  // per tile (candidates, accepted)
+  int* status;
+  int cap;     // staged-atom capacity of a tile
+  int ne_max;  // largest ext-cell count of a tile
+  LJTable lj;
+};
+
+struct PairConfig {
+  bool fp64 = false;
+  bool multi = false;   // more than one atom type
+  bool kahan = true;    // compensated FP32 force sums (mixed)
+  bool energy = false;  // potential energy and virial
+  bool count = false;   // candidate / accepted counters
+  int warps = 8;
+};
+
+int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max);
+int pair_bytes_per_atom(const PairConfig& cfg);
+cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes);  // opt-in smem attribute
+cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st);
+cudaError_t upload_own_lut(const OwnLut& lut);
+
+// ---- step.cu ----------------------------------------------------------------
+struct StepArgs {
+  const BoxDev* boxes;
+  const unsigned char* bmask;  // per global cell: bit a set when the cell is first/last of its tile on axis a
+  const int* cellS;
+  const void* Fown;
+  const void* P;
+  int64_t N;
+  bool fp64;
+};
+
+// F = Fown + halo partials, in caller order, AoS doubles (out[3*id + a]); += if accumulate.
+cudaError_t launch_forces_out(const StepArgs& s, const int* id, double* out, int accumulate, cudaStream_t st);
+// Per-box sums of the per-tile energy/virial partials (FP64, fixed order).
+cudaError_t launch_reduce_tiles(int nboxes, const int* tile0, const double* tileE, const double* tileW,
+                                double* boxE, double* boxW, cudaStream_t st);
+// Velocity-Verlet pieces.  kick: v += c_kick F / m.  With drift: x += dt v, wrap, bin.
+struct KickArgs {
+  StepArgs s;
+  double* X[3];
+  double* V[3];
+  const int* meta;
+  double ckick;  // dt or dt/2
+  double dt;
+  bool drift;
+  double hk;        // > 0: also accumulate kinetic energy at v + hk F / m
+  double* boxKE;    // per-box kinetic energy accumulators (atomicAdd of per-block sums)
+  const LJTable* ljhost;
+  LJTable lj;
+  // binning outputs (drift only)
+  int* cellOld;
+  int* slot;
+  float4* Uold;
+  int* count;
+  int* status;
+};
+cudaError_t launch_kick(const KickArgs& k, cudaStream_t st);
+cudaError_t launch_kinetic(int64_t n, const double* const V[3], const int* meta, LJTable lj, double* boxKE,
+                           cudaStream_t st);
+cudaError_t launch_scale_v(int64_t n, double* V[3], const int* meta, const double* factor, cudaStream_t st);
+cudaError_t launch_state_out(int64_t n, const double* const A[3], const int* id, double* out, cudaStream_t st);
+
+}  // namespace examd

@@ -1,0 +1,262 @@
+// step.cu -- per-atom kernels around the pair kernel: halo-partial gather,
+// velocity-Verlet kick/drift fused with the next binning, kinetic energy,
+// per-box reductions and the caller-order output.
+//
+// The reference has no integrator (one force evaluation, exaMD.f90:247-251);
+// the gather replaces its reverse force exchange, which adds received halo
+// forces into the owner's blocks (SRC/exaMD_comms.f90:330-376).  All of these
+// are HBM-bound; FP64 is used only where positions, velocities and the
+// reductions need it.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace examd {
+
+__device__ __forceinline__ void bin_store(int s, double x, double y, double z, int meta, const BoxDev& B,
+                                          int* __restrict__ cellOld, int* __restrict__ slot,
+                                          float4* __restrict__ Uold, int* __restrict__ count) {
+  // same rule as bin.cu: exact cell of the FP64 position on the grid c * bl
+  auto cell_of = [](double x, float blf, float blif, int nb, float& u) {
+    float xh = (float)x;
+    int c = (int)(xh * blif);
+    c = min(max(c, 0), nb - 1);
+    double ud = x - (double)((float)c * blf);
+    if (ud < 0.0) {
+      c = max(c - 1, 0);
+      ud = x - (double)((float)c * blf);
+    } else if (c < nb - 1 && (float)ud >= blf) {
+      if (ud >= (double)blf) {
+        c += 1;
+        ud = x - (double)((float)c * blf);
+      }
+    }
+    u = (float)ud;
+    return c;
+  };
+  float ux, uy, uz;
+  int cx = cell_of(x, B.blf, B.blif, B.nb[0], ux);
+  int cy = cell_of(y, B.blf, B.blif, B.nb[1], uy);
+  int cz = cell_of(z, B.blf, B.blif, B.nb[2], uz);
+  int gc = B.cell0 + cx + B.nb[0] * (cy + B.nb[1] * cz);
+  cellOld[s] = gc;
+  Uold[s] = make_float4(ux, uy, uz, __int_as_float(meta & 0xff));
+  slot[s] = atomicAdd(&count[gc], 1);
+}
+
+// Sum of an atom's force partials: the owning tile's, then the halo slots in
+// increasing order (fixed order: deterministic).  Mixed form: Kahan in FP32.
+__device__ __forceinline__ void gather_force(const StepArgs& a, int64_t s, double f[3]) {
+  const int m = a.bmask[a.cellS[s]];
+  if (a.fp64) {
+    const double* Fo = (const double*)a.Fown;
+    const double* P = (const double*)a.P;
+    double fx = Fo[s], fy = Fo[a.N + s], fz = Fo[2 * a.N + s];
+    for (int sl = 1; sl < 8; ++sl) {
+      if ((sl & m) != sl) continue;
+      const double* q = P + (size_t)(sl - 1) * 3 * a.N;
+      fx += q[s];
+      fy += q[a.N + s];
+      fz += q[2 * a.N + s];
+    }
+    f[0] = fx;
+    f[1] = fy;
+    f[2] = fz;
+  } else {
+    const float4* Fo = (const float4*)a.Fown;
+    const float4* P = (const float4*)a.P;
+    float4 v = Fo[s];
+    if (m == 0) {
+      f[0] = v.x;
+      f[1] = v.y;
+      f[2] = v.z;
+      return;
+    }
+    KSum kx, ky, kz;
+    kx.s = v.x;
+    ky.s = v.y;
+    kz.s = v.z;
+    for (int sl = 1; sl < 8; ++sl) {
+      if ((sl & m) != sl) continue;
+      float4 q = P[(size_t)(sl - 1) * a.N + s];
+      kx.add(q.x);
+      ky.add(q.y);
+      kz.add(q.z);
+    }
+    f[0] = (double)(kx.s - kx.c);
+    f[1] = (double)(ky.s - ky.c);
+    f[2] = (double)(kz.s - kz.c);
+  }
+}
+
+__global__ void k_forces_out(const StepArgs a, const int* __restrict__ id, double* __restrict__ out, int acc) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= a.N) return;
+  double f[3];
+  gather_force(a, s, f);
+  int64_t i = id[s];
+  if (acc) {
+    out[3 * i] += f[0];
+    out[3 * i + 1] += f[1];
+    out[3 * i + 2] += f[2];
+  } else {
+    out[3 * i] = f[0];
+    out[3 * i + 1] = f[1];
+    out[3 * i + 2] = f[2];
+  }
+}
+
+cudaError_t launch_forces_out(const StepArgs& s, const int* id, double* out, int accumulate, cudaStream_t st) {
+  if (s.N == 0) return cudaSuccess;
+  k_forces_out<<<(unsigned)((s.N + 255) / 256), 256, 0, st>>>(s, id, out, accumulate);
+  return cudaGetLastError();
+}
+
+// Per-box FP64 sums of per-tile partials: one block per box, fixed-order tree.
+__global__ void k_reduce_tiles(const int* __restrict__ tile0, const double* __restrict__ tileE,
+                               const double* __restrict__ tileW, double* __restrict__ boxE,
+                               double* __restrict__ boxW) {
+  __shared__ double se[256], sw[256];
+  const int b = blockIdx.x, t0 = tile0[b], t1 = tile0[b + 1];
+  double e = 0.0, w = 0.0;
+  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+    e += tileE[t];
+    w += tileW[t];
+  }
+  se[threadIdx.x] = e;
+  sw[threadIdx.x] = w;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      se[threadIdx.x] += se[threadIdx.x + o];
+      sw[threadIdx.x] += sw[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    boxE[b] = se[0];
+    boxW[b] = sw[0];
+  }
+}
+
+cudaError_t launch_reduce_tiles(int nboxes, const int* tile0, const double* tileE, const double* tileW,
+                                double* boxE, double* boxW, cudaStream_t st) {
+  k_reduce_tiles<<<nboxes, 256, 0, st>>>(tile0, tileE, tileW, boxE, boxW);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ void add_box_energy(double* __restrict__ boxKE, int box, double ke) {
+  const unsigned full = 0xffffffffu;
+  const int b0 = __shfl_sync(full, box, 0);
+  if (__all_sync(full, box == b0)) {
+    ke = warp_sum(ke);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&boxKE[b0], ke);
+  } else {
+    atomicAdd(&boxKE[box], ke);
+  }
+}
+
+// v += ckick F/m; optional kinetic energy at v + hk F/m; optional drift
+// x += dt v with periodic wrap followed by the binning count of the next step.
+__global__ void k_kick(const KickArgs k) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool in = s < k.s.N;
+  const int64_t ss = in ? s : 0;
+  double f[3];
+  gather_force(k.s, ss, f);
+  const int mt = k.meta[ss];
+  const int type = mt & 0xff, box = mt >> 8;
+  const double minv = k.lj.minv[type];
+  const double ck = k.ckick * minv;
+  double v[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) v[a] = k.V[a][ss];
+  if (k.hk > 0.0) {
+    const double hm = k.hk * minv;
+    double ke = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double vt = v[a] + hm * f[a];
+      ke += vt * vt;
+    }
+    ke *= 0.5 * k.lj.mass[type];
+    add_box_energy(k.boxKE, box, in ? ke : 0.0);
+  }
+  if (!in) return;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    v[a] = v[a] + ck * f[a];
+    k.V[a][s] = v[a];
+  }
+  if (k.drift) {
+    const BoxDev& B = k.s.boxes[box];
+    double x[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      x[a] = wrap_coord(k.X[a][s] + k.dt * v[a], B.L[a], B.Li[a], B.Lf[a]);
+      k.X[a][s] = x[a];
+    }
+    if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) {
+      atomicOr(k.status, ST_NONFINITE);
+      x[0] = x[1] = x[2] = 0.0;
+    }
+    bin_store((int)s, x[0], x[1], x[2], mt, B, k.cellOld, k.slot, k.Uold, k.count);
+  }
+}
+
+cudaError_t launch_kick(const KickArgs& k, cudaStream_t st) {
+  if (k.s.N == 0) return cudaSuccess;
+  k_kick<<<(unsigned)((k.s.N + 255) / 256), 256, 0, st>>>(k);
+  return cudaGetLastError();
+}
+
+__global__ void k_kinetic(int64_t n, const double* __restrict__ V0, const double* __restrict__ V1,
+                          const double* __restrict__ V2, const int* __restrict__ meta, const LJTable lj,
+                          double* __restrict__ boxKE) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool in = s < n;
+  const int64_t ss = in ? s : 0;
+  const int mt = meta[ss];
+  double ke = 0.5 * lj.mass[mt & 0xff] * (V0[ss] * V0[ss] + V1[ss] * V1[ss] + V2[ss] * V2[ss]);
+  add_box_energy(boxKE, mt >> 8, in ? ke : 0.0);
+}
+
+cudaError_t launch_kinetic(int64_t n, const double* const V[3], const int* meta, LJTable lj, double* boxKE,
+                           cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_kinetic<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, V[0], V[1], V[2], meta, lj, boxKE);
+  return cudaGetLastError();
+}
+
+__global__ void k_scale_v(int64_t n, double* __restrict__ V0, double* __restrict__ V1, double* __restrict__ V2,
+                          const int* __restrict__ meta, const double* __restrict__ factor) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double f = factor[meta[s] >> 8];
+  V0[s] *= f;
+  V1[s] *= f;
+  V2[s] *= f;
+}
+
+cudaError_t launch_scale_v(int64_t n, double* V[3], const int* meta, const double* factor, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_scale_v<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, V[0], V[1], V[2], meta, factor);
+  return cudaGetLastError();
+}
+
+__global__ void k_state_out(int64_t n, const double* __restrict__ A0, const double* __restrict__ A1,
+                            const double* __restrict__ A2, const int* __restrict__ id, double* __restrict__ out) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int64_t i = id[s];
+  out[3 * i] = A0[s];
+  out[3 * i + 1] = A1[s];
+  out[3 * i + 2] = A2[s];
+}
+
+cudaError_t launch_state_out(int64_t n, const double* const A[3], const int* id, double* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_state_out<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, A[0], A[1], A[2], id, out);
+  return cudaGetLastError();
+}
+
+}  // namespace examd

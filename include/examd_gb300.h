@@ -1,0 +1,197 @@
+/*
+ * examd_gb300.h -- C ABI of the GB300 (sm_103a) midpoint Lennard-Jones force
+ * path.  Plain C types only: pointers, sizes, a POD parameter struct.  Every
+ * entry point returns an int status (0 = EXAMD_OK); nothing throws across the
+ * boundary.  One host thread per context; calls are synchronous on the
+ * context's own CUDA stream.
+ *
+ * Reference interface this replaces:
+ *   Subroutine exaMD_forces_midpoint_all(user_func, cutoff, noprocs)
+ *     SRC/exaMD_forces.f90:308-318, called from exaMD.f90:247-251.
+ *   Its inputs are module state: grid(:,:,:)%posn/%natms (SRC/exaMD_module.f90:
+ *   34-54), globalbox/globalboxi (:54), the 63-entry interactions table
+ *   (:276-346) and the pair plug-in lennardjones_12 with its parameters
+ *   prmvdw(1,1:5) (user_func.f90:16-18,40-75).  Its output is
+ *   grid(:,:,:)%forces, accumulated (+=).
+ * The GPU replacement takes the same information as explicit arguments: the
+ * atoms gathered into one contiguous posn(3,n) array, the box, and the LJ
+ * parameters; it returns forces in the same (3,n) order plus the potential
+ * energy and virial that the reference's e12 slot was meant to carry
+ * (user_func.f90:71 leaves it zero).
+ */
+#ifndef EXAMD_GB300_H
+#define EXAMD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------
+ * 109 keeps the reference's MPI_Abort code for an atom whose block number is
+ * out of range (SRC/exaMD_module.f90:118-123).  The others are new: the
+ * reference prints and aborts (codes 101-109) or has no check at all. */
+#define EXAMD_OK 0
+#define EXAMD_ERR_OUTSIDE 109       /* position outside the box (strict mode) */
+#define EXAMD_ERR_ARG 201           /* bad argument or parameter              */
+#define EXAMD_ERR_NB_TOO_SMALL 202  /* fewer than 5 cells on an axis          */
+#define EXAMD_ERR_CELL_OVERFLOW 203 /* a tile's staged atoms exceed capacity  */
+#define EXAMD_ERR_NONFINITE 204     /* NaN/Inf position or force              */
+#define EXAMD_ERR_TIMEOUT 205       /* a bounded device wait gave up          */
+#define EXAMD_ERR_CUDA 206          /* CUDA runtime error                     */
+#define EXAMD_ERR_NOMEM 207         /* device or pinned allocation failed     */
+#define EXAMD_ERR_STATE 208         /* call order (e.g. no atoms set)         */
+#define EXAMD_ERR_NO_DEVICE 209     /* no CUDA device / wrong architecture    */
+
+#define EXAMD_MAX_TYPES 4
+
+/* Precision forms. */
+#define EXAMD_FP64 0  /* FP64 end to end                                       */
+#define EXAMD_MIXED 1 /* FP32 pair forces on tile-frame offsets, Kahan-merged  */
+                      /* FP32 per-atom sums, FP64 integration/wrap/reductions  */
+
+typedef struct examd_params {
+  int precision;      /* EXAMD_FP64 or EXAMD_MIXED                            */
+  int ntypes;         /* 1..EXAMD_MAX_TYPES                                   */
+  /* ntypes x ntypes tables, row-major [a*ntypes+b], symmetric.  eps = prmvdw
+   * (1,1), sigma = prmvdw(1,2), rc = prmvdw(1,5) for the single-type case. */
+  double eps[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];
+  double sigma[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];
+  double rc[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];
+  double mass[EXAMD_MAX_TYPES]; /* 0 = 1.0                                     */
+  /* block_length: the cell edge, >= max(rc)/2; 0 = max(rc)/2 as the reference
+   * (exaMD.f90:56).  Rounded up to the nearest value with at most 14
+   * significant bits so that every cell origin c*block_length is exact in
+   * FP32.  nb = Int(L/block_length) cells per axis with the last cell
+   * absorbing the remainder (SRC/exaMD_utils.f90:179,
+   * SRC/exaMD_module.f90:109-113). */
+  double cell_edge;
+  int tile[3];        /* home cells per CTA tile per axis; 0 = default        */
+  int warps;          /* warps per CTA in the pair kernel; 0 = default        */
+  int strict_box;     /* 1: positions outside [0,L) are an error (109);       */
+                      /* 0: they are wrapped periodically                     */
+  int device;         /* CUDA device ordinal                                  */
+} examd_params;
+
+/* One independent periodic box of a batched ensemble. */
+typedef struct examd_box {
+  double L[3];
+  int64_t natoms;
+} examd_box;
+
+typedef struct examd_stats {
+  double epot;     /* potential energy, FP64 reduction                        */
+  double virial;   /* W = sum over pairs of r_ij . f_ij                       */
+  double ekin;     /* kinetic energy after the last step                      */
+  int64_t steps;   /* steps taken                                             */
+  double ms;       /* device time of the call, CUDA events                    */
+} examd_stats;
+
+typedef struct examd_ctx examd_ctx;
+
+/* Fill *p with the reference defaults: FP64, one type, eps = sigma = 1,
+ * rc = 2.5, reference cell rule, default tiles. */
+void examd_default_params(examd_params *p);
+
+/* Create a context for nboxes independent boxes (1 for the reference's single
+ * domain).  Fails with EXAMD_ERR_NB_TOO_SMALL if any box has fewer than 5
+ * cells on an axis: with 4 or fewer, separations +2 and -2 name the same cell
+ * pair and the 63-entry table would count it twice. */
+int examd_gpu_create(const examd_params *params, int nboxes,
+                     const examd_box *boxes, examd_ctx **out);
+void examd_gpu_destroy(examd_ctx *ctx);
+
+/* Upload atoms.  pos: 3*n doubles, posn(3,n) order, boxes concatenated in
+ * order; n must equal the sum of the boxes' natoms.  type: n ints or NULL
+ * (all type 0).  vel: 3*n doubles or NULL (zero). */
+int examd_gpu_set_atoms(examd_ctx *ctx, int64_t n, const double *pos,
+                        const int *type, const double *vel);
+
+/* One force evaluation at the current positions: the drop-in for
+ * exaMD_forces_midpoint_all.  forces: 3*n doubles in the caller's atom order,
+ * overwritten (accumulate = 0) or added to (accumulate = 1, the reference's
+ * += semantics).  epot, virial: per-box arrays of nboxes doubles, or NULL. */
+int examd_gpu_forces(examd_ctx *ctx, double *forces, double *epot,
+                     double *virial, int accumulate);
+
+/* Same as examd_gpu_forces but with new positions given in the same call
+ * (one host->device copy, the pair path, one device->host copy). */
+int examd_gpu_forces_at(examd_ctx *ctx, const double *pos, double *forces,
+                        double *epot, double *virial, int accumulate);
+
+/* nsteps velocity-Verlet steps of size dt (rebinning every step).  When
+ * graph_chunk > 0 the step loop is captured once as a CUDA graph of
+ * graph_chunk steps and replayed.  energies: when non-NULL, per-box
+ * (ekin, epot) pairs after every step: nsteps * nboxes * 2 doubles. */
+int examd_gpu_run(examd_ctx *ctx, int nsteps, double dt, int graph_chunk,
+                  double *energies, examd_stats *stats);
+
+/* Current positions and velocities in the caller's order (3*n each, NULL to
+ * skip). */
+int examd_gpu_get_state(examd_ctx *ctx, double *pos, double *vel);
+
+/* Per-box kinetic energy (sum m v^2 / 2) at the current velocities. */
+int examd_gpu_kinetic(examd_ctx *ctx, double *ekin);
+
+/* Scale all velocities of box b by factor[b] (thermostat / melt protocol). */
+int examd_gpu_scale_velocities(examd_ctx *ctx, const double *factor);
+
+/* Device time in ms of `reps` force evaluations (positions already resident),
+ * measured with CUDA events on the context's stream.  kernel_ms, when
+ * non-NULL, receives the average duration of the pair kernel alone. */
+int examd_gpu_time_forces(examd_ctx *ctx, int reps, double *ms,
+                          double *kernel_ms);
+
+/* Counters of the last force evaluation: candidate pairs (the reference's
+ * particle-interaction calls), accepted pairs (r <= rc), tiles, and the
+ * largest staged atom count of a tile.  Any pointer may be NULL. */
+int examd_gpu_counters(examd_ctx *ctx, int64_t *candidates, int64_t *accepted,
+                       int64_t *tiles, int64_t *max_tile_atoms);
+
+/* Introspection (no counterpart in the reference): the row structure and the
+ * per-position-class ownership masks the pair kernel derives from the 63-entry
+ * table (SRC/exaMD_module.f90:276-346).  rows: 13*2 (dy, dz); lut: 125*13
+ * masks over dx = -2..2.  Host-only; returns EXAMD_ERR_ARG if the table does
+ * not have the expected shape. */
+int examd_own_table(signed char *rows, unsigned char *lut);
+
+/* Text of a status code; never NULL. */
+const char *examd_gpu_strerror(int code);
+
+/* Last CUDA error text seen by the context (empty if none). */
+const char *examd_gpu_last_error(examd_ctx *ctx);
+
+/* Page-locked host buffers for fast copies (cudaHostAlloc). */
+int examd_host_alloc(void **ptr, int64_t bytes);
+int examd_host_free(void *ptr);
+
+/* ---- input generators (host code, no device use) ------------------------ */
+
+/* FCC lattice of 4*nc^3 atoms at density rho, box edge L = nc*(4/rho)^(1/3).
+ * pos: 3*4*nc^3 doubles.  Returns the box edge in *L. */
+int examd_gen_fcc(int nc, double rho, double *pos, double *L);
+
+/* Maxwell-Boltzmann velocities at temperature T (k_B = 1) with zero net
+ * momentum and the kinetic temperature rescaled to exactly T
+ * (3(n-1) degrees of freedom).  mass: per-type masses or NULL (1). */
+int examd_gen_velocities(int64_t n, const int *type, const double *mass,
+                         double T, uint64_t seed, double *vel);
+
+/* Uniform random positions in [lo, hi) of a box L with a minimum pair
+ * separation dmin enforced by rejection against a cell grid (periodic).  The
+ * first n_fixed atoms of pos are already placed and are kept.  Returns
+ * EXAMD_ERR_ARG if an atom could not be placed in max_tries attempts. */
+int examd_gen_random(int64_t n, int64_t n_fixed, const double L[3],
+                     const double lo[3], const double hi[3], double dmin,
+                     uint64_t seed, int64_t max_tries, double *pos);
+
+/* Simple-cubic lattice of m^3 atoms at density rho with uniform jitter of
+ * amplitude jitter*a per coordinate; types drawn with P(type 1) = frac_b. */
+int examd_gen_jittered_sc(int m, double rho, double jitter, double frac_b,
+                          uint64_t seed, double *pos, int *type, double *L);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
