@@ -169,6 +169,8 @@ struct examd_ctx {
   double* stage2 = nullptr;  // 3N doubles
   int* d_meta_in = nullptr;
   double* d_factor = nullptr;
+  int64_t* d_atom0 = nullptr;
+  double* keAtom = nullptr;
   int ebuf_steps = 0;
 
   bool atoms_set = false;
@@ -212,7 +214,8 @@ void free_all(examd_ctx* ctx) {
   void* ptrs[] = {ctx->d_boxes, ctx->d_tiles, ctx->d_tile0, ctx->d_bmask, ctx->U, ctx->Uold, ctx->cellS,
                   ctx->cellOld, ctx->slot, ctx->src, ctx->count, ctx->cstart, ctx->bsum, ctx->d_total,
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
-                  ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor};
+                  ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor,
+                  ctx->d_atom0, ctx->keAtom};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (int b = 0; b < 2; ++b) {
@@ -553,6 +556,8 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   ALLOC(ctx->stage2, 3 * N);
   ALLOC(ctx->d_meta_in, N);
   ALLOC(ctx->d_factor, nboxes);
+  ALLOC(ctx->d_atom0, nboxes + 1);
+  ALLOC(ctx->keAtom, N);
 #undef ALLOC
   cudaStream_t st = ctx->st;
   bool ok = cudaMemcpyAsync(ctx->d_boxes, ctx->bh.data(), nboxes * sizeof(BoxDev), cudaMemcpyHostToDevice, st) ==
@@ -562,6 +567,8 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
             cudaMemcpyAsync(ctx->d_tile0, ctx->tile0.data(), (nboxes + 1) * sizeof(int), cudaMemcpyHostToDevice,
                             st) == cudaSuccess &&
             cudaMemcpyAsync(ctx->d_bmask, bmask.data(), NC, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(ctx->d_atom0, ctx->atom0.data(), (nboxes + 1) * sizeof(int64_t),
+                            cudaMemcpyHostToDevice, st) == cudaSuccess &&
             cudaMemsetAsync(ctx->count, 0, NC * sizeof(int), st) == cudaSuccess &&
             cudaMemsetAsync(ctx->status, 0, sizeof(int), st) == cudaSuccess &&
             cudaStreamSynchronize(st) == cudaSuccess;
@@ -805,6 +812,9 @@ KickArgs kick_args(examd_ctx* ctx, double ckick, double dt, bool drift, double h
   k.drift = drift;
   k.hk = hk;
   k.boxKE = boxKE;
+  k.keAtom = ctx->keAtom;
+  k.atom0 = ctx->d_atom0;
+  k.nboxes = ctx->nboxes;
   k.lj = ctx->lj;
   k.cellOld = ctx->cellOld;
   k.slot = ctx->slot;
@@ -865,7 +875,6 @@ int examd_gpu_run(examd_ctx* ctx, int nsteps, double dt, int graph_chunk, double
   const double h = 0.5 * dt;
   CK(cudaEventRecord(ctx->e0, st));
   // step 1: half kick + drift, then forces
-  if (wantE) CK(cudaMemsetAsync(ctx->boxKE, 0, (size_t)(ctx->ebuf_steps + 1) * nb * sizeof(double), st));
   rc = step_once(ctx, h, dt, nullptr, wantE ? ctx->boxE : nullptr, wantE ? ctx->boxW : nullptr);
   if (rc) return rc;
   if (wantE) {
@@ -886,7 +895,6 @@ int examd_gpu_run(examd_ctx* ctx, int nsteps, double dt, int graph_chunk, double
         const int parity = ctx->cur;
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        if (wantE) cudaMemsetAsync(ctx->boxKE, 0, (size_t)(chunk + 1) * nb * sizeof(double), st);
         int src = EXAMD_OK;
         for (int j = 0; j < chunk && src == EXAMD_OK; ++j)
           src = step_once(ctx, dt, dt, wantE ? ctx->boxKE + (size_t)j * nb : nullptr,
@@ -927,10 +935,7 @@ int examd_gpu_run(examd_ctx* ctx, int nsteps, double dt, int graph_chunk, double
       if (rc) return rc;
     } else {
       double* ke = nullptr;
-      if (wantE) {
-        CK(cudaMemsetAsync(ctx->boxKE, 0, nb * sizeof(double), st));
-        ke = ctx->boxKE;
-      }
+      if (wantE) ke = ctx->boxKE;
       rc = step_once(ctx, dt, dt, ke, wantE ? ctx->boxE : nullptr, wantE ? ctx->boxW : nullptr);
       if (rc) return rc;
       if (wantE)
@@ -945,7 +950,6 @@ int examd_gpu_run(examd_ctx* ctx, int nsteps, double dt, int graph_chunk, double
     }
   }
   // closing half kick: v(t_n) = v(t_n - h) + h F/m
-  if (wantE) CK(cudaMemsetAsync(ctx->boxKE, 0, nb * sizeof(double), st));
   CK(launch_kick(kick_args(ctx, h, dt, false, wantE ? h : 0.0, ctx->boxKE), st));
   if (wantE)
     for (int b = 0; b < nb; ++b)
@@ -994,8 +998,8 @@ int examd_gpu_kinetic(examd_ctx* ctx, double* ekin) {
   if (!ctx->atoms_set) return EXAMD_ERR_STATE;
   cudaSetDevice(ctx->dev);
   const int c = ctx->cur;
-  CK(cudaMemsetAsync(ctx->boxKE, 0, ctx->nboxes * sizeof(double), ctx->st));
-  CK(launch_kinetic(ctx->N, ctx->V[c], ctx->meta[c], ctx->lj, ctx->boxKE, ctx->st));
+  CK(launch_kinetic(ctx->N, ctx->nboxes, ctx->d_atom0, ctx->V[c], ctx->meta[c], ctx->lj, ctx->keAtom, ctx->boxKE,
+                    ctx->st));
   CK(cudaMemcpyAsync(ekin, ctx->boxKE, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   return EXAMD_OK;

@@ -87,9 +87,11 @@ struct KickArgs {
   double ckick;  // dt or dt/2
   double dt;
   bool drift;
-  double hk;        // > 0: also accumulate kinetic energy at v + hk F / m
-  double* boxKE;    // per-box kinetic energy accumulators (atomicAdd of per-block sums)
-  const LJTable* ljhost;
+  double hk;        // > 0: also the kinetic energy at v + hk F / m, per box
+  double* keAtom;   // per-atom kinetic energy scratch (N)
+  double* boxKE;    // per-box kinetic energy (fixed-order reduction of keAtom)
+  const int64_t* atom0;  // nboxes + 1 atom offsets (sorted order is grouped by box)
+  int nboxes;
   LJTable lj;
   // binning outputs (drift only)
   int* cellOld;
@@ -99,8 +101,9 @@ struct KickArgs {
   int* status;
 };
 cudaError_t launch_kick(const KickArgs& k, cudaStream_t st);
-cudaError_t launch_kinetic(int64_t n, const double* const V[3], const int* meta, LJTable lj, double* boxKE,
-                           cudaStream_t st);
+cudaError_t launch_kinetic(int64_t n, int nboxes, const int64_t* atom0, const double* const V[3], const int* meta,
+                           LJTable lj, double* keAtom, double* boxKE, cudaStream_t st);
+cudaError_t launch_reduce_atoms(int nboxes, const int64_t* atom0, const double* v, double* out, cudaStream_t st);
 cudaError_t launch_scale_v(int64_t n, double* V[3], const int* meta, const double* factor, cudaStream_t st);
 cudaError_t launch_state_out(int64_t n, const double* const A[3], const int* id, double* out, cudaStream_t st);
 

@@ -144,15 +144,28 @@ cudaError_t launch_reduce_tiles(int nboxes, const int* tile0, const double* tile
   return cudaGetLastError();
 }
 
-__device__ __forceinline__ void add_box_energy(double* __restrict__ boxKE, int box, double ke) {
-  const unsigned full = 0xffffffffu;
-  const int b0 = __shfl_sync(full, box, 0);
-  if (__all_sync(full, box == b0)) {
-    ke = warp_sum(ke);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&boxKE[b0], ke);
-  } else {
-    atomicAdd(&boxKE[box], ke);
+// Per-box sums of a per-atom quantity over the boxes' contiguous atom ranges
+// (atoms are sorted by box): one block per box, fixed assignment and tree
+// order, so the result is reproducible bit for bit.
+__global__ void k_reduce_atoms(const int64_t* __restrict__ atom0, const double* __restrict__ v,
+                               double* __restrict__ out) {
+  __shared__ double sh[256];
+  const int b = blockIdx.x;
+  const int64_t a0 = atom0[b], a1 = atom0[b + 1];
+  double s = 0.0;
+  for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) s += v[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) out[b] = sh[0];
+}
+
+cudaError_t launch_reduce_atoms(int nboxes, const int64_t* atom0, const double* v, double* out, cudaStream_t st) {
+  k_reduce_atoms<<<nboxes, 256, 0, st>>>(atom0, v, out);
+  return cudaGetLastError();
 }
 
 // v += ckick F/m; optional kinetic energy at v + hk F/m; optional drift
@@ -179,7 +192,7 @@ __global__ void k_kick(const KickArgs k) {
       ke += vt * vt;
     }
     ke *= 0.5 * k.lj.mass[type];
-    add_box_energy(k.boxKE, box, in ? ke : 0.0);
+    if (in) k.keAtom[s] = ke;
   }
   if (!in) return;
 #pragma unroll
@@ -204,26 +217,23 @@ __global__ void k_kick(const KickArgs k) {
 }
 
 cudaError_t launch_kick(const KickArgs& k, cudaStream_t st) {
-  if (k.s.N == 0) return cudaSuccess;
-  k_kick<<<(unsigned)((k.s.N + 255) / 256), 256, 0, st>>>(k);
+  if (k.s.N > 0) k_kick<<<(unsigned)((k.s.N + 255) / 256), 256, 0, st>>>(k);
+  if (k.hk > 0.0) k_reduce_atoms<<<k.nboxes, 256, 0, st>>>(k.atom0, k.keAtom, k.boxKE);
   return cudaGetLastError();
 }
 
 __global__ void k_kinetic(int64_t n, const double* __restrict__ V0, const double* __restrict__ V1,
                           const double* __restrict__ V2, const int* __restrict__ meta, const LJTable lj,
-                          double* __restrict__ boxKE) {
+                          double* __restrict__ keAtom) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const bool in = s < n;
-  const int64_t ss = in ? s : 0;
-  const int mt = meta[ss];
-  double ke = 0.5 * lj.mass[mt & 0xff] * (V0[ss] * V0[ss] + V1[ss] * V1[ss] + V2[ss] * V2[ss]);
-  add_box_energy(boxKE, mt >> 8, in ? ke : 0.0);
+  if (s >= n) return;
+  keAtom[s] = 0.5 * lj.mass[meta[s] & 0xff] * (V0[s] * V0[s] + V1[s] * V1[s] + V2[s] * V2[s]);
 }
 
-cudaError_t launch_kinetic(int64_t n, const double* const V[3], const int* meta, LJTable lj, double* boxKE,
-                           cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_kinetic<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, V[0], V[1], V[2], meta, lj, boxKE);
+cudaError_t launch_kinetic(int64_t n, int nboxes, const int64_t* atom0, const double* const V[3], const int* meta,
+                           LJTable lj, double* keAtom, double* boxKE, cudaStream_t st) {
+  if (n > 0) k_kinetic<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, V[0], V[1], V[2], meta, lj, keAtom);
+  k_reduce_atoms<<<nboxes, 256, 0, st>>>(atom0, keAtom, boxKE);
   return cudaGetLastError();
 }
 
