@@ -86,7 +86,7 @@ def load():
             "examd_gpu_kinetic": (C.c_int, [ctxp, dp]),
             "examd_gpu_scale_velocities": (C.c_int, [ctxp, dp]),
             "examd_gpu_time_forces": (C.c_int, [ctxp, C.c_int, dp, dp]),
-            "examd_gpu_counters": (C.c_int, [ctxp, i64p, i64p, i64p, i64p]),
+            "examd_gpu_counters": (C.c_int, [ctxp, i64p, i64p, i64p, i64p, i64p]),
             "examd_gpu_strerror": (C.c_char_p, [C.c_int]),
             "examd_gpu_last_error": (C.c_char_p, [ctxp]),
             "examd_own_table": (C.c_int, [C.POINTER(C.c_byte), C.POINTER(C.c_ubyte)]),

@@ -184,10 +184,11 @@ class MidpointLJ:
         return ms.value, kms.value
 
     def counters(self):
-        c, a, t, m = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
-        self._chk(self._lib.examd_gpu_counters(self._ctx, C.byref(c), C.byref(a), C.byref(t), C.byref(m)),
-                  "examd_gpu_counters")
-        return dict(candidates=c.value, accepted=a.value, tiles=t.value, max_tile_atoms=m.value)
+        c, a, e, t, m = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        self._chk(self._lib.examd_gpu_counters(self._ctx, C.byref(c), C.byref(a), C.byref(e), C.byref(t),
+                                               C.byref(m)), "examd_gpu_counters")
+        return dict(candidates=c.value, accepted=a.value, evaluated=e.value, tiles=t.value,
+                    max_tile_atoms=m.value)
 
 
 def forces_midpoint_all(pos, box, cutoff, eps=1.0, sigma=1.0, forces=None, precision=FP64, energy=False, **kw):

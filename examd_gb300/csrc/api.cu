@@ -93,6 +93,7 @@ bool build_own_lut(OwnLut& L) {
           }
           if (r == kRows - 1 && class_ok(cx, 0) && class_ok(cy, 0) && class_ok(cz, 0)) mask |= 1u << 2;
           L.lut[cls][r] = (unsigned char)mask;
+          if (mask) L.rowact[cy * 5 + cz] |= (unsigned short)(1u << r);
         }
       }
   return true;
@@ -366,7 +367,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     delete ctx;
     return EXAMD_ERR_ARG;
   }
-  const int deftile = ctx->pc.fp64 ? 4 : 6;
+  const int deftile = 4;
   int T[3];
   for (int a = 0; a < 3; ++a) {
     T[a] = p.tile[a] > 0 ? p.tile[a] : deftile;
@@ -393,6 +394,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     rc2max = std::max(rc2max, lj.p32[k].rc2);
   }
   lj.rc2max = rc2max;
+  lj.prune2 = (float)((rcmax + 1e-4) * (rcmax + 1e-4));
   for (int a = 0; a < EXAMD_MAX_TYPES; ++a) {
     double m = (a < nt && p.mass[a] > 0) ? p.mass[a] : 1.0;
     lj.mass[a] = m;
@@ -546,7 +548,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   }
   ALLOC(ctx->tileE, ctx->ntiles);
   ALLOC(ctx->tileW, ctx->ntiles);
-  ALLOC(ctx->tileC, 2 * (size_t)ctx->ntiles);
+  ALLOC(ctx->tileC, 3 * (size_t)ctx->ntiles);
   ALLOC(ctx->boxE, nboxes);
   ALLOC(ctx->boxW, nboxes);
   ALLOC(ctx->boxKE, nboxes);
@@ -1040,14 +1042,14 @@ int examd_gpu_time_forces(examd_ctx* ctx, int reps, double* ms, double* kernel_m
   return EXAMD_OK;
 }
 
-int examd_gpu_counters(examd_ctx* ctx, int64_t* candidates, int64_t* accepted, int64_t* tiles,
-                       int64_t* max_tile_atoms) {
+int examd_gpu_counters(examd_ctx* ctx, int64_t* candidates, int64_t* accepted, int64_t* evaluated,
+                       int64_t* tiles, int64_t* max_tile_atoms) {
   if (!ctx) return EXAMD_ERR_ARG;
   if (!ctx->atoms_set) return EXAMD_ERR_STATE;
   cudaSetDevice(ctx->dev);
   int rc = run_pair(ctx, false, true);
   if (rc) return rc;
-  std::vector<long long> c(2 * (size_t)ctx->ntiles);
+  std::vector<long long> c(3 * (size_t)ctx->ntiles);
   CK(cudaMemcpyAsync(c.data(), ctx->tileC, c.size() * sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
   int occ = 0;
   CK(cudaMemsetAsync(ctx->d_occ, 0, 2 * sizeof(int), ctx->st));
@@ -1057,13 +1059,15 @@ int examd_gpu_counters(examd_ctx* ctx, int64_t* candidates, int64_t* accepted, i
   CK(cudaStreamSynchronize(ctx->st));
   rc = check_status(ctx);
   if (rc) return rc;
-  long long s1 = 0, s2 = 0;
+  long long s1 = 0, s2 = 0, s3 = 0;
   for (int t = 0; t < ctx->ntiles; ++t) {
-    s1 += c[2 * t];
-    s2 += c[2 * t + 1];
+    s1 += c[3 * t];
+    s2 += c[3 * t + 1];
+    s3 += c[3 * t + 2];
   }
   if (candidates) *candidates = s1;
   if (accepted) *accepted = s2;
+  if (evaluated) *evaluated = s3;
   if (tiles) *tiles = ctx->ntiles;
   if (max_tile_atoms) *max_tile_atoms = occ;
   ctx->forces_valid = true;

@@ -55,6 +55,7 @@ struct LJ64 {
 struct LJTable {
   int nt;
   float rc2max;
+  float prune2;  // (max rc + 1e-4)^2: cell boxes farther than this hold no pair
   LJ32 p32[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];
   LJ64 p64[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];
   double minv[EXAMD_MAX_TYPES];
@@ -69,6 +70,9 @@ struct LJTable {
 struct OwnLut {
   signed char rows[kRows][2];
   unsigned char lut[kClasses][kRows];
+  // rowact[cy*5+cz] bit r: some x-class of a row with y/z classes (cy, cz)
+  // owns a pair in row r (lets a warp skip whole rows)
+  unsigned short rowact[25];
 };
 
 __host__ __device__ inline int pos_class(int l, int t) {

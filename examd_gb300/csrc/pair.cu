@@ -4,26 +4,33 @@
 // interaction and lennardjones_12 (SRC/exaMD_forces.f90:41-551,
 // user_func.f90:40-75).  A tile owns every cell pair whose home block -- given
 // by the reference's 63-entry table (SRC/exaMD_module.f90:276-346) -- lies in
-// the tile; the tile plus a one-cell halo is staged in shared memory (periodic
-// images folded into the staged coordinates: the HBM/SMEM counterpart of the
-// MPI halo exchange in SRC/exaMD_comms.f90:44-244).
+// the tile; the tile plus a one-cell halo is staged in shared memory with the
+// periodic images folded into the staged coordinates (the SMEM counterpart of
+// the MPI halo exchange, SRC/exaMD_comms.f90:44-244).
 //
-// Work order.  The 62 non-self table entries are, per home-relative cell A,
-// 12 full x-rows of 5 cells (dy, dz fixed, dx = -2..2) plus the half row
-// dx = +1, +2; with the self pairs that is 13 "rows" r.  Phase r: each warp
-// takes chunks of 32 consecutive staged i-atoms from its own block of x-rows;
-// lane l owns atom i = c0 + l and the contiguous j-ranges of the cells in row
-// r that the table assigns to this tile (ownership masks per position class).
-// The warp walks the ranges along diagonals: at step k lane l handles
-// j = l + k, so no two lanes touch the same j at once and the Newton's-third-
-// law update of f_j is a plain shared-memory read-modify-write: deterministic
-// and free of atomics.  Warps own disjoint x-rows, and a phase shifts every
-// row by the same (dy, dz), so warps never share j atoms inside a phase;
-// phases are separated by __syncthreads().
+// Work order.  The 62 non-self table entries are, per cell A, 12 full x-rows
+// of 5 cells (dy, dz fixed, dx = -2..2) plus the half row dx = +1, +2; with
+// the pairs inside A that makes 13 "rows" r.  The work units of a tile are
+// (row r, 32 consecutive staged atoms); unit u goes to warp u mod W.  A warp
+// turns each atom of a unit into an item: the contiguous j-ranges of the cells
+// of row r that the table assigns to this tile (ownership masks per position
+// class), trimmed to the cells whose box comes within rc of the atom (the
+// accepted pairs are unchanged).  Atoms without work are dropped and the items
+// are compacted into passes of 32 lanes.  A lane walks its own j-ranges: the
+// i-side partial sum stays in registers, the j-side terms (Newton's third
+// law) are added as they come.
 //
-// Output: the forces of the tile's home atoms go to Fown, those of halo atoms
-// to the partial slot P[s] (s = bitmask of the axes on which the copy is a
-// halo copy); the integrator sums an atom's 1..8 partials in a fixed order.
+// Accumulation.  Mixed form: each per-atom force component is an exact 32-bit
+// fixed-point sum in shared memory (scale 2^15, native integer atomics), so
+// the result does not depend on the order of the terms and is reproducible
+// bit for bit; a term of magnitude >= 1024 (r < 0.79 sigma at eps = 1) takes
+// an FP32 side path instead, which keeps every fixed-point sum of up to 63
+// terms inside 2^31.  FP64 form: FP64 shared-memory atomics.  No global
+// atomics are used.
+//
+// Output: forces of the tile's home atoms go to Fown, those of halo copies to
+// the partial slot P[s] (s = bitmask of the axes on which the copy is a halo
+// copy); the integrator sums an atom's 1..8 partials in a fixed order.
 #include <climits>
 
 #include "common.cuh"
@@ -35,38 +42,48 @@ __constant__ OwnLut c_own;
 
 cudaError_t upload_own_lut(const OwnLut& lut) { return cudaMemcpyToSymbol(c_own, &lut, sizeof(OwnLut)); }
 
+constexpr int kDT = 6;        // origin differences for d = -2..3
+constexpr int kItems = 64;    // per-warp item buffer
+constexpr float kFix = 32768.f;        // fixed-point scale 2^15
+constexpr float kFixInv = 1.f / 32768.f;
+constexpr float kFixMax = 1024.f;      // larger terms take the FP32 side path
+
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
-  int lstart, gfirst, rowb, ox, oy, oz, dyt, dzt, imx, imy, imz, red;
-  int pf, fi, fj, fic, fjc, px, gidx, code;
+  int lstart, gfirst, ox, oy, oz, dyt, dzt, imx, imy, imz, red, lut, rows, items;
+  int pf, fa, fr, px, gidx, code;
   int bytes;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
-__host__ __device__ inline Layout make_layout(bool fp64, bool kahan, int cap, int ne_max, int nw) {
+__host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int nw) {
   Layout L;
   int o = 0;
   L.lstart = o; o = align16(o + 4 * (ne_max + 1));
   L.gfirst = o; o = align16(o + 4 * ne_max);
-  L.rowb = o;   o = align16(o + 4 * (nw + 1));
-  L.ox = o;     o = align16(o + 4 * kMaxExt);
-  L.oy = o;     o = align16(o + 4 * kMaxExt);
-  L.oz = o;     o = align16(o + 4 * kMaxExt);
-  L.dyt = o;    o = align16(o + 4 * kMaxExt * 5);
-  L.dzt = o;    o = align16(o + 4 * kMaxExt * 5);
+  L.ox = o;     o = align16(o + 4 * (kMaxExt + 1));
+  L.oy = o;     o = align16(o + 4 * (kMaxExt + 1));
+  L.oz = o;     o = align16(o + 4 * (kMaxExt + 1));
+  L.dyt = o;    o = align16(o + 4 * kMaxExt * kDT);
+  L.dzt = o;    o = align16(o + 4 * kMaxExt * kDT);
   L.imx = o;    o = align16(o + 8 * kMaxExt);
   L.imy = o;    o = align16(o + 8 * kMaxExt);
   L.imz = o;    o = align16(o + 8 * kMaxExt);
   L.red = o;    o = align16(o + 8 * 4 * nw);
-  const int fs = fp64 ? 8 : 4;
+  L.lut = o;    o = align16(o + kClasses * kRows);
+  L.rows = o;   o = align16(o + 2 * kRows);
+  L.items = o;  o = align16(o + 16 * kItems * nw);
   L.pf = o;     o = align16(o + 16 * cap);
-  L.fi = o;     o = align16(o + 3 * fs * cap);
-  L.fj = o;     o = align16(o + 3 * fs * cap);
-  const bool comp = kahan && !fp64;
-  L.fic = o;    o = align16(o + (comp ? 3 * 4 * cap : 0));
-  L.fjc = o;    o = align16(o + (comp ? 3 * 4 * cap : 0));
-  L.px = o;     o = align16(o + (fp64 ? 3 * 8 * cap : 0));
+  if (fp64) {
+    L.fa = o;   o = align16(o + 3 * 8 * cap);  // FP64 force sums
+    L.fr = o;
+    L.px = o;   o = align16(o + 3 * 8 * cap);  // FP64 positions
+  } else {
+    L.fa = o;   o = align16(o + 3 * 4 * cap);  // fixed-point force sums
+    L.fr = o;   o = align16(o + 3 * 4 * cap);  // FP32 side path for large terms
+    L.px = o;
+  }
   L.gidx = o;   o = align16(o + 4 * cap);
   L.code = o;   o = align16(o + 2 * cap);
   L.bytes = o;
@@ -74,28 +91,102 @@ __host__ __device__ inline Layout make_layout(bool fp64, bool kahan, int cap, in
 }
 
 int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max) {
-  return make_layout(cfg.fp64, cfg.kahan, cap, ne_max, cfg.warps).bytes;
+  return make_layout(cfg.fp64, cap, ne_max, cfg.warps).bytes;
 }
-int pair_bytes_per_atom(const PairConfig& cfg) {
-  return make_layout(cfg.fp64, cfg.kahan, 1024, 0, 1).bytes / 1024;
+int pair_bytes_per_atom(const PairConfig& cfg) { return make_layout(cfg.fp64, 1024, 0, 1).bytes / 1024; }
+
+// Tile geometry and shared tables seen by the item builder.
+struct TileView {
+  int EX, EY, EZ, tx, ty, tz;
+  const int* lstart;
+  const float *ox, *oy, *oz;
+  const float4* pf;
+  const unsigned short* code;
+  const unsigned char* lut;
+  const signed char* rows;
+  float prune2;
+  bool fp64;
+};
+
+// j-ranges of atom i for row r: [lo1, lo1+n1) and [lo2, lo2+n2) in staged
+// order.  ncand (COUNT) gets the reference's candidate count of the item.
+__device__ __forceinline__ void make_item(const TileView& T, int i, int r, int& lo1, int& n1, int& lo2, int& n2,
+                                          int* ncand) {
+  lo1 = n1 = lo2 = n2 = 0;
+  const int ci = T.code[i];
+  const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
+  int mask = T.lut[(pos_class(lx - 1, T.tx) * 25 + pos_class(ly - 1, T.ty) * 5 + pos_class(lz - 1, T.tz)) * kRows + r];
+  if (!mask) return;
+  const int dy = T.rows[2 * r], dz = T.rows[2 * r + 1];
+  const int rowbase = ((ly + dy) + T.EY * (lz + dz)) * T.EX + lx - 2;  // + bit b -> ext cell of dx = b - 2
+  if (ncand) {  // every atom of the owned cells, as the reference visits them
+    for (int b = 0; b < 5; ++b)
+      if ((mask >> b) & 1) {
+        const int e = rowbase + b;
+        *ncand += (r == kRows - 1 && b == 2) ? T.lstart[e + 1] - i - 1 : T.lstart[e + 1] - T.lstart[e];
+      }
+  }
+  // distance from the atom to the cell boxes (tile frame, FP32; the 1e-4
+  // margin in prune2 covers the rounding)
+  const float4 pi = T.pf[i];
+  const float py = T.fp64 ? pi.y : T.oy[ly] + pi.y;
+  const float pz = T.fp64 ? pi.z : T.oz[lz] + pi.z;
+  const float gy = dy > 0 ? T.oy[ly + dy] - py : (dy < 0 ? py - T.oy[ly + dy + 1] : 0.f);
+  const float gz = dz > 0 ? T.oz[lz + dz] - pz : (dz < 0 ? pz - T.oz[lz + dz + 1] : 0.f);
+  const float g2 = fmaxf(gy, 0.f) * fmaxf(gy, 0.f) + fmaxf(gz, 0.f) * fmaxf(gz, 0.f);
+  if (g2 > T.prune2) return;
+#pragma unroll
+  for (int b = 0; b < 5; ++b) {
+    if (b == 2 || !((mask >> b) & 1)) continue;
+    const int dx = b - 2;
+    const float gx = dx > 0 ? T.ox[lx + dx] - pi.x : pi.x - T.ox[lx + dx + 1];
+    if (gx > 0.f && fmaf(gx, gx, g2) > T.prune2) mask &= ~(1 << b);
+  }
+  if (!mask) return;
+  const int b0 = __ffs(mask) - 1;
+  int b1 = b0;
+  while (b1 < 4 && ((mask >> (b1 + 1)) & 1)) ++b1;
+  lo1 = T.lstart[rowbase + b0];
+  n1 = T.lstart[rowbase + b1 + 1] - lo1;
+  if (r == kRows - 1 && b0 == 2) {  // pairs inside A: a2 > a1
+    n1 -= i + 1 - lo1;
+    lo1 = i + 1;
+  }
+  const int m2 = mask & ~((2 << b1) - 1);
+  if (m2) {
+    const int c0b = __ffs(m2) - 1, c1b = 31 - __clz(m2);
+    lo2 = T.lstart[rowbase + c0b];
+    n2 = T.lstart[rowbase + c1b + 1] - lo2;
+  }
+  if (n1 <= 0) {
+    lo1 = lo2;
+    n1 = n2;
+    lo2 = 0;
+    n2 = 0;
+  }
+  n1 = max(n1, 0);
+  n2 = max(n2, 0);
 }
 
-template <bool FP64>
-struct Acc;
-template <>
-struct Acc<false> {
-  using T = float;
-};
-template <>
-struct Acc<true> {
-  using T = double;
-};
+// Add an FP32 force term to atom m: exact fixed point, or the side path for a
+// term too large for it.
+__device__ __forceinline__ void add_fixed(int* fa, float* fr, int cap, int m, float fx, float fy, float fz,
+                                          int* status) {
+  if (fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) < kFixMax) {
+    atomicAdd(&fa[m], __float2int_rn(fx * kFix));
+    atomicAdd(&fa[cap + m], __float2int_rn(fy * kFix));
+    atomicAdd(&fa[2 * cap + m], __float2int_rn(fz * kFix));
+  } else {
+    atomicAdd(&fr[m], fx);
+    atomicAdd(&fr[cap + m], fy);
+    atomicAdd(&fr[2 * cap + m], fz);
+  }
+}
 
-template <bool FP64, bool MULTI, bool KAHAN, bool ENERGY, bool COUNT>
+template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
 __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
-  using T = typename Acc<FP64>::T;
-  constexpr bool COMP = KAHAN && !FP64;
   extern __shared__ __align__(16) unsigned char smem[];
+  const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   const int tile = blockIdx.x;
   const int4 t0 = A.tiles[2 * tile], t1 = A.tiles[2 * tile + 1];
@@ -104,10 +195,9 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
   const int tx = t1.x, ty = t1.y, tz = t1.z;
   const int EX = tx + 2, EY = ty + 2, EZ = tz + 2;
   const int NE = EX * EY * EZ, NR = EY * EZ;
-  const Layout L = make_layout(FP64, KAHAN, A.cap, A.ne_max, nw);
+  const Layout L = make_layout(FP64, A.cap, A.ne_max, nw);
   int* lstart = (int*)(smem + L.lstart);
   int* gfirst = (int*)(smem + L.gfirst);
-  int* rowb = (int*)(smem + L.rowb);
   float* ox = (float*)(smem + L.ox);
   float* oy = (float*)(smem + L.oy);
   float* oz = (float*)(smem + L.oz);
@@ -117,17 +207,14 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
   double* imy = (double*)(smem + L.imy);
   double* imz = (double*)(smem + L.imz);
   double* red = (double*)(smem + L.red);
+  unsigned char* slut = (unsigned char*)(smem + L.lut);
+  signed char* srows = (signed char*)(smem + L.rows);
   float4* pf = (float4*)(smem + L.pf);
-  T* fi = (T*)(smem + L.fi);
-  T* fj = (T*)(smem + L.fj);
-  float* fic = (float*)(smem + L.fic);
-  float* fjc = (float*)(smem + L.fjc);
-  double* pd = (double*)(smem + L.px);
   int* gidx = (int*)(smem + L.gidx);
   unsigned short* code = (unsigned short*)(smem + L.code);
   const int cap = A.cap;
 
-  // (1) ext cells: global cell, count, first atom
+  // (1) ext cells: global cell, count, first atom; ownership tables to smem
   for (int e = tid; e < NE; e += blockDim.x) {
     int lx = e % EX, rr = e / EX, ly = rr % EY, lz = rr / EY;
     int gx = X0 + lx - 1, gy = Y0 + ly - 1, gz = Z0 + lz - 1;
@@ -142,10 +229,13 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
     gfirst[e] = s0;
     lstart[e] = A.cstart[gc + 1] - s0;
   }
-  // Per-axis tables.  Ext coordinate l (0-based; cell X0 + l - 1) has origin
-  // g*bl + n*L, g the wrapped cell, n its periodic image.  Tile-frame origins
-  // are taken relative to the tile centre; dyt/dzt hold the exact origin
-  // difference between ext rows l and l + d (d = -2..2), rounded once.
+  for (int k = tid; k < kClasses * kRows; k += blockDim.x) slut[k] = c_own.lut[k / kRows][k % kRows];
+  if (tid < 2 * kRows) srows[tid] = c_own.rows[tid >> 1][tid & 1];
+  // Per-axis tables.  Ext coordinate l (cell X0 + l - 1, l = 0..E; l = E is
+  // the far edge of the last ext cell) has origin g*bl + n*L, g the wrapped
+  // cell and n its periodic image.  o*[l]: origin relative to the tile centre
+  // (FP32).  d*t[l*6 + d + 2]: exact origin difference between ext rows l and
+  // l + d rounded once (d = -2..3).  im*[l]: n*L (FP64).
   {
     const int a = tid >> 5, l = tid & 31;
     if (a < 3) {
@@ -153,29 +243,26 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
       const int g0 = a == 0 ? X0 : (a == 1 ? Y0 : Z0);
       const int t = a == 0 ? tx : (a == 1 ? ty : tz);
       const int nb = B.nb[a];
-      if (l < E) {
-        int g = g0 + l - 1, n = 0;
+      auto origin = [&](int ll) {
+        int g = g0 + ll - 1, n = 0;
         if (g < 0) { g += nb; n = -1; }
         if (g >= nb) { g -= nb; n = 1; }
-        double org = (double)((float)g * B.blf) + n * B.L[a];
-        double centre = (double)((float)g0 * B.blf) + 0.5 * t * B.bl;
-        float o = (float)(org - centre);
-        (a == 0 ? ox : (a == 1 ? oy : oz))[l] = o;
-        (a == 0 ? imx : (a == 1 ? imy : imz))[l] = n * B.L[a];
-        if (a > 0) {
-          float* dt = a == 1 ? dyt : dzt;
+        return (double)((float)g * B.blf) + n * B.L[a];
+      };
+      if (l <= E) {
+        const double org = origin(l);
+        const double centre = (double)((float)g0 * B.blf) + 0.5 * t * B.bl;
+        (a == 0 ? ox : (a == 1 ? oy : oz))[l] = (float)(org - centre);
+        if (l < E) {
+          int g = g0 + l - 1;
+          (a == 0 ? imx : (a == 1 ? imy : imz))[l] = g < 0 ? -B.L[a] : (g >= nb ? B.L[a] : 0.0);
+          if (a > 0) {
+            float* dt = a == 1 ? dyt : dzt;
 #pragma unroll
-          for (int d = -2; d <= 2; ++d) {
-            int l2 = l + d;
-            float v = 0.f;
-            if (l2 >= 0 && l2 < E) {
-              int g2 = g0 + l2 - 1, n2 = 0;
-              if (g2 < 0) { g2 += nb; n2 = -1; }
-              if (g2 >= nb) { g2 -= nb; n2 = 1; }
-              double org2 = (double)((float)g2 * B.blf) + n2 * B.L[a];
-              v = (float)(org2 - org);
+            for (int d = -2; d <= 3; ++d) {
+              const int l2 = l + d;
+              dt[l * kDT + d + 2] = (l2 >= 0 && l2 <= E) ? (float)(origin(l2) - org) : 0.f;
             }
-            dt[l * 5 + d + 2] = v;
           }
         }
       }
@@ -192,7 +279,7 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
     int x = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, o);
+      int y = __shfl_up_sync(FULL, x, o);
       if (lane >= o) x += y;
     }
     int* wsum = (int*)red;
@@ -218,24 +305,19 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
         A.tileW[tile] = 0.0;
       }
       if (COUNT) {
-        A.tileC[2 * tile] = 0;
-        A.tileC[2 * tile + 1] = 0;
+        A.tileC[3 * tile] = 0;
+        A.tileC[3 * tile + 1] = 0;
+        A.tileC[3 * tile + 2] = 0;
       }
     }
     return;
   }
-  // (3) warp row blocks balanced by atoms; rows never split across warps
-  if (tid <= nw) {
-    long target = (long)tid * total / nw;
-    int lo = 0, hi = NR;  // first row R with start(R) >= target
-    while (lo < hi) {
-      int mid = (lo + hi) >> 1;
-      if (lstart[mid * EX] >= target) hi = mid;
-      else lo = mid + 1;
-    }
-    rowb[tid] = (tid == nw) ? NR : lo;
-  }
-  // (4) stage atoms row by row
+  // (3) stage atoms row by row (a row of ext cells is contiguous in HBM
+  // unless it wraps)
+  int* fa = (int*)(smem + L.fa);
+  float* fr = (float*)(smem + L.fr);
+  double* fd = (double*)(smem + L.fa);
+  double* pd = (double*)(smem + L.px);
   for (int R = warp; R < NR; R += nw) {
     const int e0 = R * EX, a0 = lstart[e0], a1 = lstart[e0 + EX];
     const int ly = R % EY, lz = R / EY;
@@ -245,206 +327,188 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
       const int e = e0 + lx;
       const int g = gfirst[e] + (t - lstart[e]);
       const float4 u = A.U[g];
-      float4 p;
       if (FP64) {
-        p = make_float4(ox[lx] + u.x, oy[ly] + u.y, oz[lz] + u.z, u.w);
+        pf[t] = make_float4(ox[lx] + u.x, oy[ly] + u.y, oz[lz] + u.z, u.w);
         pd[t] = A.X0[g];
         pd[cap + t] = A.X1[g];
         pd[2 * cap + t] = A.X2[g];
-      } else {
-        p = make_float4(ox[lx] + u.x, u.y, u.z, u.w);
-      }
-      pf[t] = p;
-      gidx[t] = g;
-      code[t] = (unsigned short)(lx | (ly << 5) | (lz << 10));
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        fi[c * cap + t] = T(0);
-        fj[c * cap + t] = T(0);
-        if (COMP) {
-          fic[c * cap + t] = 0.f;
-          fjc[c * cap + t] = 0.f;
+        for (int c = 0; c < 3; ++c) fd[c * cap + t] = 0.0;
+      } else {
+        pf[t] = make_float4(ox[lx] + u.x, u.y, u.z, u.w);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          fa[c * cap + t] = 0;
+          fr[c * cap + t] = 0.f;
         }
       }
+      gidx[t] = g;
+      code[t] = (unsigned short)(lx | (ly << 5) | (lz << 10));
     }
   }
   __syncthreads();
 
-  const int ib = lstart[rowb[warp] * EX], ie = lstart[rowb[warp + 1] * EX];
+  const TileView TV{EX, EY, EZ, tx, ty, tz, lstart, ox, oy, oz, pf, code, slut, srows, A.lj.prune2, FP64};
   const LJ32 q32 = A.lj.p32[0];
   const LJ64 q64 = A.lj.p64[0];
   const float rcpre = A.lj.rc2max * 1.0001f + 1e-4f;  // FP32 prefilter of the FP64 form
-  T esum = T(0), wsum = T(0);
-  KSum ek, wk;
-  int ncand = 0, nacc = 0;
+  double esum = 0.0, wsum = 0.0;  // FP64 form
+  KSum ek, wk;                    // mixed form: Kahan merge of per-pass FP32 sums
+  int ncand = 0, neval = 0, nacc = 0;
+  // per-warp item buffer: int4 (i | r << 16, lo1, lo2, n1 | n2 << 16)
+  int4* items = (int4*)(smem + L.items) + warp * kItems;
+  const unsigned lt = (1u << lane) - 1u;
+  const int nch = (total + 31) >> 5;
+  const int nunits = kRows * nch;
+  int nbuf = 0;
 
-  for (int r = 0; r < kRows; ++r) {
-    const int dy = c_own.rows[r][0], dz = c_own.rows[r][1];
-    for (int c0 = ib; c0 < ie; c0 += 32) {
-      const int i = c0 + lane;
-      const bool vi = i < ie;
-      const int ci = vi ? code[i] : 0;
-      const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;  // 0-based ext coords
-      int mask = 0;
-      if (vi)
-        mask = c_own.lut[pos_class(lx - 1, tx) * 25 + pos_class(ly - 1, ty) * 5 + pos_class(lz - 1, tz)][r];
-      if (__ballot_sync(0xffffffffu, mask != 0) == 0u) continue;
+  for (int u = warp;; u += nw) {
+    const bool more = u < nunits;
+    if (more) {  // unit (r, chunk): items of 32 consecutive staged atoms for row r
+      const int r = u / nch, i = (u - r * nch) * 32 + lane;
       int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
-      if (mask) {
-        const int rowbase = ((ly + dy) + EY * (lz + dz)) * EX + lx - 2;  // + bit b -> ext cell of dx = b - 2
-        const int b0 = __ffs(mask) - 1;
-        int b1 = b0;
-        while (b1 < 4 && ((mask >> (b1 + 1)) & 1)) ++b1;
-        lo1 = lstart[rowbase + b0];
-        const int hi1 = lstart[rowbase + b1 + 1];
-        if (r == kRows - 1 && b0 == 2) lo1 = i + 1;  // pairs inside A: a2 > a1
-        n1 = hi1 - lo1;
-        const int m2 = mask & ~((2 << b1) - 1);
-        if (m2) {
-          const int c0b = __ffs(m2) - 1, c1b = 31 - __clz(m2);
-          lo2 = lstart[rowbase + c0b];
-          n2 = lstart[rowbase + c1b + 1] - lo2;
+      if (i < total) make_item(TV, i, r, lo1, n1, lo2, n2, COUNT ? &ncand : nullptr);
+      const unsigned b = __ballot_sync(FULL, n1 > 0);
+      if (n1 > 0) items[nbuf + __popc(b & lt)] = make_int4(i | (r << 16), lo1, lo2, n1 | (n2 << 16));
+      nbuf += __popc(b);
+      __syncwarp();
+      if (nbuf < 32) continue;
+    } else if (nbuf == 0) {
+      break;
+    }
+    // ---- one pass: one item per lane, each lane walks its own j-ranges ----
+    const int cnt = min(nbuf, 32);
+    int i = -1, r = 0, lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
+    if (lane < cnt) {
+      const int4 it = items[lane];
+      i = it.x & 0xffff;
+      r = it.x >> 16;
+      lo1 = it.y;
+      lo2 = it.z;
+      n1 = it.w & 0xffff;
+      n2 = it.w >> 16;
+    }
+    const int nt = n1 + n2;
+    const int tmax = warp_max(nt);
+    const float4 pi = pf[i >= 0 ? i : 0];
+    const int ci = code[i >= 0 ? i : 0];
+    const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
+    const int dy = srows[2 * r], dz = srows[2 * r + 1];
+    const int ti = __float_as_int(pi.w);
+    if (!FP64) {
+      const float Cx = -pi.x;
+      const float Cy = dyt[ly * kDT + dy + 2] - pi.y;
+      const float Cz = dzt[lz * kDT + dz + 2] - pi.z;
+      float ax = 0.f, ay = 0.f, az = 0.f, ea = 0.f, wa = 0.f;
+      for (int t = 0; t < tmax; ++t) {
+        if (t < nt) {
+          const int m = t < n1 ? lo1 + t : lo2 + (t - n1);
+          const float4 q = pf[m];
+          if (COUNT) ++neval;
+          const float dxv = q.x + Cx, dyv = q.y + Cy, dzv = q.z + Cz;
+          const float r2 = fmaf(dxv, dxv, fmaf(dyv, dyv, dzv * dzv));
+          LJ32 P = q32;
+          if (MULTI) P = A.lj.p32[ti * A.lj.nt + __float_as_int(q.w)];
+          if (r2 <= P.rc2) {
+            const float ri = rcp_approx(r2);
+            const float s2 = P.sig2 * ri;
+            const float s6 = s2 * s2 * s2;
+            const float dg = P.m24eps * s6 * fmaf(2.f, s6, -1.f) * ri;
+            ax = fmaf(dg, dxv, ax);
+            ay = fmaf(dg, dyv, ay);
+            az = fmaf(dg, dzv, az);
+            add_fixed(fa, fr, cap, m, -dg * dxv, -dg * dyv, -dg * dzv, A.status);
+            if (ENERGY) {
+              ea = fmaf(P.c4eps * s6, s6 - 1.f, ea);
+              wa = fmaf(-dg, r2, wa);
+            }
+            if (COUNT) ++nacc;
+          }
         }
       }
-      int kmn = INT_MAX, kmx = INT_MIN;
-      if (n1 > 0) { kmn = lo1 - lane; kmx = lo1 + n1 - 1 - lane; }
-      if (n2 > 0) { kmn = min(kmn, lo2 - lane); kmx = max(kmx, lo2 + n2 - 1 - lane); }
-      kmn = warp_min(kmn);
-      kmx = warp_max(kmx);
-      if (kmn > kmx) continue;
-
-      const float4 pi = pf[vi ? i : 0];
-      const int ti = __float_as_int(pi.w);
-      // per-lane constants of this row: d = p_j + C
-      float Cx = -pi.x, Cy, Cz;
+      if (nt > 0) {
+        add_fixed(fa, fr, cap, i, ax, ay, az, A.status);
+        if (ENERGY) {
+          ek.add(ea);
+          wk.add(wa);
+        }
+      }
+    } else {
+      // FP32 prefilter on tile-frame coordinates, then the reference's FP64
+      // arithmetic (SRC/exaMD_forces.f90:509-523, user_func.f90:52-69)
       double xi = 0, yi = 0, zi = 0, sy = 0, sz = 0, sxi = 0;
-      if (FP64) {
-        Cy = -pi.y;
-        Cz = -pi.z;
-        xi = pd[vi ? i : 0];
-        yi = pd[cap + (vi ? i : 0)];
-        zi = pd[2 * cap + (vi ? i : 0)];
+      if (i >= 0) {
+        xi = pd[i];
+        yi = pd[cap + i];
+        zi = pd[2 * cap + i];
         const int lyj = min(max(ly + dy, 0), EY - 1), lzj = min(max(lz + dz, 0), EZ - 1);
         sy = imy[lyj] - imy[ly];
         sz = imz[lzj] - imz[lz];
         sxi = imx[lx];
-      } else {
-        Cy = dyt[ly * 5 + dy + 2] - pi.y;
-        Cz = dzt[lz * 5 + dz + 2] - pi.z;
       }
-      T ax = T(0), ay = T(0), az = T(0);
-      KSum kx, ky, kz;
-
-      for (int k = kmn; k <= kmx; ++k) {
-        const int m = lane + k;
-        const bool v = ((unsigned)(m - lo1) < (unsigned)n1) | ((unsigned)(m - lo2) < (unsigned)n2);
-        if (v) {
+      double ax = 0, ay = 0, az = 0;
+      for (int t = 0; t < tmax; ++t) {
+        if (t < nt) {
+          const int m = t < n1 ? lo1 + t : lo2 + (t - n1);
           const float4 q = pf[m];
-          if (COUNT) ++ncand;
-          if (!FP64) {
-            const float dx = q.x + Cx, dyv = q.y + Cy, dzv = q.z + Cz;
-            const float r2 = fmaf(dx, dx, fmaf(dyv, dyv, dzv * dzv));
-            LJ32 P = q32;
-            if (MULTI) P = A.lj.p32[ti * A.lj.nt + __float_as_int(q.w)];
-            if (r2 <= P.rc2) {
-              const float ri = rcp_approx(r2);
-              const float s2 = P.sig2 * ri;
-              const float s6 = s2 * s2 * s2;
-              const float dg = P.m24eps * s6 * fmaf(2.f, s6, -1.f) * ri;
-              const float fx = dg * dx, fy = dg * dyv, fz = dg * dzv;
-              if (COMP) {
-                kx.add(fx);
-                ky.add(fy);
-                kz.add(fz);
-                float* sj = (float*)fj;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                  const float f = c == 0 ? -fx : (c == 1 ? -fy : -fz);
-                  float s = sj[c * cap + m], cc = fjc[c * cap + m];
-                  float y = f - cc, t = s + y;
-                  fjc[c * cap + m] = (t - s) - y;
-                  sj[c * cap + m] = t;
-                }
-              } else {
-                ax += fx;
-                ay += fy;
-                az += fz;
-                fj[m] -= fx;
-                fj[cap + m] -= fy;
-                fj[2 * cap + m] -= fz;
-              }
+          if (COUNT) ++neval;
+          const float fxp = q.x - pi.x, fyp = q.y - pi.y, fzp = q.z - pi.z;
+          const float r2f = fmaf(fxp, fxp, fmaf(fyp, fyp, fzp * fzp));
+          if (r2f <= rcpre) {
+            const int lxj = code[m] & 31;
+            const double sx = imx[lxj] - sxi;
+            double dx = __dsub_rn(pd[m], xi);
+            double dyv = __dsub_rn(pd[cap + m], yi);
+            double dzv = __dsub_rn(pd[2 * cap + m], zi);
+            // periodic image: physical separation = (x_j - x_i) + (n_j - n_i) L,
+            // exact (Sterbenz), equal to the reference's dx - Nint(dx/L) L
+            if (sx != 0.0) dx = __dadd_rn(dx, sx);
+            if (sy != 0.0) dyv = __dadd_rn(dyv, sy);
+            if (sz != 0.0) dzv = __dadd_rn(dzv, sz);
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dyv, dyv)), __dmul_rn(dzv, dzv));
+            LJ64 P = q64;
+            if (MULTI) P = A.lj.p64[ti * A.lj.nt + __float_as_int(q.w)];
+            if (d2 <= P.rc2) {
+              const double d2i = __drcp_rn(d2);
+              const double tt = __dmul_rn(P.sig2, d2i);
+              const double d6 = __dmul_rn(__dmul_rn(tt, tt), tt);
+              const double d12 = __dmul_rn(d6, d6);
+              const double dg = -__dmul_rn(__dmul_rn(P.eps24, __dsub_rn(__dmul_rn(2.0, d12), d6)), d2i);
+              const double fx = __dmul_rn(dg, dx), fy = __dmul_rn(dg, dyv), fz = __dmul_rn(dg, dzv);
+              ax += fx;
+              ay += fy;
+              az += fz;
+              atomicAdd(&fd[m], -fx);
+              atomicAdd(&fd[cap + m], -fy);
+              atomicAdd(&fd[2 * cap + m], -fz);
               if (ENERGY) {
-                ek.add(P.c4eps * s6 * (s6 - 1.f));
-                wk.add(-dg * r2);
+                esum += __dmul_rn(P.eps4, __dsub_rn(d12, d6));
+                wsum += -__dmul_rn(dg, d2);
               }
               if (COUNT) ++nacc;
             }
-          } else {
-            // FP32 prefilter on tile-frame coordinates, then the reference's
-            // FP64 arithmetic (SRC/exaMD_forces.f90:509-523, user_func.f90:52-69)
-            const float fxp = q.x - pi.x, fyp = q.y - pi.y, fzp = q.z - pi.z;
-            const float r2f = fmaf(fxp, fxp, fmaf(fyp, fyp, fzp * fzp));
-            if (r2f <= rcpre) {
-              const int lxj = code[m] & 31;
-              const double sx = imx[lxj] - sxi;
-              double dx = __dsub_rn(pd[m], xi);
-              double dyv = __dsub_rn(pd[cap + m], yi);
-              double dzv = __dsub_rn(pd[2 * cap + m], zi);
-              // periodic image: physical separation = (x_j - x_i) + (n_j - n_i) L,
-              // exact (Sterbenz), equal to the reference's dx - Nint(dx/L) L
-              if (sx != 0.0) dx = __dadd_rn(dx, sx);
-              if (sy != 0.0) dyv = __dadd_rn(dyv, sy);
-              if (sz != 0.0) dzv = __dadd_rn(dzv, sz);
-              const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dyv, dyv)), __dmul_rn(dzv, dzv));
-              LJ64 P = q64;
-              if (MULTI) P = A.lj.p64[ti * A.lj.nt + __float_as_int(q.w)];
-              if (d2 <= P.rc2) {
-                const double d2i = __drcp_rn(d2);
-                const double t = __dmul_rn(P.sig2, d2i);
-                const double d6 = __dmul_rn(__dmul_rn(t, t), t);
-                const double d12 = __dmul_rn(d6, d6);
-                const double dg = -__dmul_rn(__dmul_rn(P.eps24, __dsub_rn(__dmul_rn(2.0, d12), d6)), d2i);
-                const double fx = __dmul_rn(dg, dx), fy = __dmul_rn(dg, dyv), fz = __dmul_rn(dg, dzv);
-                ax += fx;
-                ay += fy;
-                az += fz;
-                fj[m] -= fx;
-                fj[cap + m] -= fy;
-                fj[2 * cap + m] -= fz;
-                if (ENERGY) {
-                  esum += __dmul_rn(P.eps4, __dsub_rn(d12, d6));
-                  wsum += -__dmul_rn(dg, d2);
-                }
-                if (COUNT) ++nacc;
-              }
-            }
           }
         }
-        __syncwarp();
       }
-      if (vi) {
-        if (COMP) {
-          float* si = (float*)fi;
-          const float part[3] = {kx.s - kx.c, ky.s - ky.c, kz.s - kz.c};
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            float s = si[c * cap + i], cc = fic[c * cap + i];
-            float y = part[c] - cc, t = s + y;
-            fic[c * cap + i] = (t - s) - y;
-            si[c * cap + i] = t;
-          }
-        } else {
-          fi[i] += ax;
-          fi[cap + i] += ay;
-          fi[2 * cap + i] += az;
-        }
+      if (nt > 0) {
+        atomicAdd(&fd[i], ax);
+        atomicAdd(&fd[cap + i], ay);
+        atomicAdd(&fd[2 * cap + i], az);
       }
-      __syncwarp();
     }
-    __syncthreads();
+    // drop the processed items
+    __syncwarp();
+    const int rem = nbuf - cnt;
+    int4 keep = make_int4(0, 0, 0, 0);
+    if (lane < rem) keep = items[32 + lane];
+    __syncwarp();
+    if (lane < rem) items[lane] = keep;
+    nbuf = rem;
+    __syncwarp();
   }
+  __syncthreads();
 
-  // (5) write-back: home atoms -> Fown, halo copies -> P[slot]
+  // (4) write-back: home atoms -> Fown, halo copies -> P[slot]
   for (int t = tid; t < total; t += blockDim.x) {
     const int ci = code[t];
     const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
@@ -454,34 +518,23 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
     if (FP64) {
       double* F = slot == 0 ? (double*)A.Fown : (double*)A.P + (size_t)(slot - 1) * 3 * A.N;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) F[c * A.N + g] = (double)fi[c * cap + t] + (double)fj[c * cap + t];
+      for (int c = 0; c < 3; ++c) F[c * A.N + g] = fd[c * cap + t];
     } else {
       float f[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        if (COMP) {
-          KSum k;
-          k.s = ((float*)fi)[c * cap + t];
-          k.c = fic[c * cap + t];
-          k.add(((float*)fj)[c * cap + t]);
-          k.add(-fjc[c * cap + t]);
-          f[c] = k.s - k.c;
-        } else {
-          f[c] = (float)fi[c * cap + t] + (float)fj[c * cap + t];
-        }
-      }
+      for (int c = 0; c < 3; ++c) f[c] = fmaf((float)fa[c * cap + t], kFixInv, fr[c * cap + t]);
       float4* F = slot == 0 ? (float4*)A.Fown : (float4*)A.P + (size_t)(slot - 1) * A.N;
       F[g] = make_float4(f[0], f[1], f[2], 0.f);
     }
   }
 
-  // (6) per-tile energy / virial / counters
+  // (5) per-tile energy / virial / counters
   if (ENERGY || COUNT) {
     double e = 0.0, w = 0.0;
     if (ENERGY) {
       if (FP64) {
-        e = (double)esum;
-        w = (double)wsum;
+        e = esum;
+        w = wsum;
       } else {
         e = (double)ek.s - (double)ek.c;
         w = (double)wk.s - (double)wk.c;
@@ -489,7 +542,8 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
     }
     e = warp_sum(e);
     w = warp_sum(w);
-    long long c1 = warp_sum((long long)ncand), c2 = warp_sum((long long)nacc);
+    const long long c1 = warp_sum((long long)ncand), c2 = warp_sum((long long)nacc),
+                    c3 = warp_sum((long long)neval);
     __syncthreads();
     if (lane == 0) {
       red[4 * warp] = e;
@@ -511,35 +565,40 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
         A.tileW[tile] = sw;
       }
       if (COUNT) {
-        A.tileC[2 * tile] = (long long)s1;
-        A.tileC[2 * tile + 1] = (long long)s2;
+        A.tileC[3 * tile] = (long long)s1;
+        A.tileC[3 * tile + 1] = (long long)s2;
+      }
+    }
+    if (COUNT) {
+      __syncthreads();
+      if (lane == 0) red[warp] = (double)c3;
+      __syncthreads();
+      if (tid == 0) {
+        double s3 = 0;
+        for (int k = 0; k < nw; ++k) s3 += red[k];
+        A.tileC[3 * tile + 2] = (long long)s3;
       }
     }
   }
 }
 
-template <bool FP64, bool MULTI, bool KAHAN, bool ENERGY, bool COUNT>
+template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
 static void* kfn() {
-  return (void*)&k_pair<FP64, MULTI, KAHAN, ENERGY, COUNT>;
+  return (void*)&k_pair<FP64, MULTI, ENERGY, COUNT>;
 }
 
 static void* pick(const PairConfig& c) {
-  // FP64 ignores KAHAN; instantiate the combinations that are used.
-#define EXAMD_PICK(F, M, K)                                              \
-  if (c.energy && c.count) return kfn<F, M, K, true, true>();            \
-  if (c.energy) return kfn<F, M, K, true, false>();                      \
-  if (c.count) return kfn<F, M, K, false, true>();                       \
-  return kfn<F, M, K, false, false>();
+#define EXAMD_PICK(F, M)                                               \
+  if (c.energy && c.count) return kfn<F, M, true, true>();            \
+  if (c.energy) return kfn<F, M, true, false>();                      \
+  if (c.count) return kfn<F, M, false, true>();                       \
+  return kfn<F, M, false, false>();
   if (c.fp64) {
-    if (c.multi) { EXAMD_PICK(true, true, false) }
-    EXAMD_PICK(true, false, false)
+    if (c.multi) { EXAMD_PICK(true, true) }
+    EXAMD_PICK(true, false)
   }
-  if (c.multi) {
-    if (c.kahan) { EXAMD_PICK(false, true, true) }
-    EXAMD_PICK(false, true, false)
-  }
-  if (c.kahan) { EXAMD_PICK(false, false, true) }
-  EXAMD_PICK(false, false, false)
+  if (c.multi) { EXAMD_PICK(false, true) }
+  EXAMD_PICK(false, false)
 #undef EXAMD_PICK
 }
 

@@ -143,11 +143,15 @@ int examd_gpu_scale_velocities(examd_ctx *ctx, const double *factor);
 int examd_gpu_time_forces(examd_ctx *ctx, int reps, double *ms,
                           double *kernel_ms);
 
-/* Counters of the last force evaluation: candidate pairs (the reference's
- * particle-interaction calls), accepted pairs (r <= rc), tiles, and the
- * largest staged atom count of a tile.  Any pointer may be NULL. */
+/* Counters of one force evaluation at the current positions: candidate pairs
+ * (the reference's particle-interaction calls: every atom pair of every owned
+ * cell pair, SRC/exaMD_forces.f90:349-377), accepted pairs (r <= rc),
+ * evaluated pairs (distance tests the kernel actually ran after skipping cells
+ * beyond rc), tiles, and the largest staged atom count of a tile.  Any
+ * pointer may be NULL. */
 int examd_gpu_counters(examd_ctx *ctx, int64_t *candidates, int64_t *accepted,
-                       int64_t *tiles, int64_t *max_tile_atoms);
+                       int64_t *evaluated, int64_t *tiles,
+                       int64_t *max_tile_atoms);
 
 /* Introspection (no counterpart in the reference): the row structure and the
  * per-position-class ownership masks the pair kernel derives from the 63-entry
