@@ -50,8 +50,8 @@ constexpr float kFixMax = 1024.f;      // larger terms take the FP32 side path
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
-  int lstart, gfirst, ox, oy, oz, dyt, dzt, imx, imy, imz, red, lut, rows, items;
-  int pf, fa, fr, px, gidx, code;
+  int lstart, gfirst, ox, oy, oz, dyt, dzt, imx, imy, imz, red, lut, rows, items, queue;
+  int pf, fa, fr, px, code;
   int bytes;
 };
 
@@ -70,10 +70,11 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.imx = o;    o = align16(o + 8 * kMaxExt);
   L.imy = o;    o = align16(o + 8 * kMaxExt);
   L.imz = o;    o = align16(o + 8 * kMaxExt);
-  L.red = o;    o = align16(o + 8 * 4 * nw);
+  L.red = o;    o = align16(o + 8 * 8 * nw + 16);  // + the CTA's unit counter
   L.lut = o;    o = align16(o + kClasses * kRows);
   L.rows = o;   o = align16(o + 2 * kRows);
   L.items = o;  o = align16(o + 16 * kItems * nw);
+  L.queue = o;  o = align16(o + (fp64 ? 0 : 20 * kItems * nw));
   L.pf = o;     o = align16(o + 16 * cap);
   if (fp64) {
     L.fa = o;   o = align16(o + 3 * 8 * cap);  // FP64 force sums
@@ -84,7 +85,6 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
     L.fr = o;   o = align16(o + 3 * 4 * cap);  // FP32 side path for large terms
     L.px = o;
   }
-  L.gidx = o;   o = align16(o + 4 * cap);
   L.code = o;   o = align16(o + 2 * cap);
   L.bytes = o;
   return L;
@@ -168,23 +168,68 @@ __device__ __forceinline__ void make_item(const TileView& T, int i, int r, int& 
   n2 = max(n2, 0);
 }
 
-// Add an FP32 force term to atom m: exact fixed point, or the side path for a
-// term too large for it.
-__device__ __forceinline__ void add_fixed(int* fa, float* fr, int cap, int m, float fx, float fy, float fz,
-                                          int* status) {
-  if (fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) < kFixMax) {
-    atomicAdd(&fa[m], __float2int_rn(fx * kFix));
-    atomicAdd(&fa[cap + m], __float2int_rn(fy * kFix));
-    atomicAdd(&fa[2 * cap + m], __float2int_rn(fz * kFix));
+// Add a force term, given already multiplied by the fixed-point scale, to
+// atom m: exact fixed point, or the FP32 side path for a term too large for it.
+__device__ __forceinline__ void add_fixed(int* fa, float* fr, int cap, int m, float fx, float fy, float fz) {
+  if (fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) < kFixMax * kFix) {
+    atomicAdd(&fa[m], __float2int_rn(fx));
+    atomicAdd(&fa[cap + m], __float2int_rn(fy));
+    atomicAdd(&fa[2 * cap + m], __float2int_rn(fz));
   } else {
-    atomicAdd(&fr[m], fx);
-    atomicAdd(&fr[cap + m], fy);
-    atomicAdd(&fr[2 * cap + m], fz);
+    atomicAdd(&fr[m], fx * kFixInv);
+    atomicAdd(&fr[cap + m], fy * kFixInv);
+    atomicAdd(&fr[2 * cap + m], fz * kFixInv);
+  }
+}
+
+// Exact sum of FP32 terms in 64-bit fixed point (2^-32 resolution): the total
+// does not depend on the order of the terms.  A term of magnitude >= 30000
+// (a pair closer than ~0.46 sigma) goes to an FP32 side sum.
+struct FixSum {
+  long long v = 0;
+  float side = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    if (fabsf(x) < 30000.f) {
+      const float hs = x * 65536.f;  // exact power-of-two scaling
+      const int h = __float2int_rz(hs);
+      const int l = __float2int_rn((hs - (float)h) * 65536.f);  // hs - h is exact
+      v += ((long long)h << 16) + l;
+    } else {
+      side += x;
+    }
+  }
+};
+
+// Forces of cnt queued accepted pairs, one per lane: entry = (d = x_j - x_i,
+// r^2) and key = i | j << 14 | type_i << 28 | type_j << 30.  user_func.f90:58-69
+// in FP32: dg = -24 eps (2 s^12 - s^6) / r^2, f_i += dg d, f_j -= dg d.
+template <bool MULTI, bool ENERGY>
+__device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int* qk, int* fa, float* fr, int cap,
+                                            const LJTable& lj, FixSum& ek, FixSum& wk) {
+  const int lane = threadIdx.x & 31;
+  if (lane < cnt) {
+    const float4 d = qd[lane];
+    const unsigned key = (unsigned)qk[lane];
+    const int i = key & 0x3fff, m = (key >> 14) & 0x3fff;
+    LJ32 P = lj.p32[0];
+    if (MULTI) P = lj.p32[((key >> 28) & 3) * lj.nt + (key >> 30)];
+    const float ri = rcp_approx(d.w);
+    const float s2 = P.sig2 * ri;
+    const float s6 = s2 * s2 * s2;
+    const float dg = P.m24eps * s6 * fmaf(2.f, s6, -1.f) * ri;
+    const float dgs = kFix * dg;
+    const float fx = dgs * d.x, fy = dgs * d.y, fz = dgs * d.z;
+    add_fixed(fa, fr, cap, i, fx, fy, fz);
+    add_fixed(fa, fr, cap, m, -fx, -fy, -fz);
+    if (ENERGY) {
+      ek.add(P.c4eps * s6 * (s6 - 1.f));
+      wk.add(-dg * d.w);
+    }
   }
 }
 
 template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
-__global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
+__global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -210,7 +255,6 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
   unsigned char* slut = (unsigned char*)(smem + L.lut);
   signed char* srows = (signed char*)(smem + L.rows);
   float4* pf = (float4*)(smem + L.pf);
-  int* gidx = (int*)(smem + L.gidx);
   unsigned short* code = (unsigned short*)(smem + L.code);
   const int cap = A.cap;
 
@@ -342,41 +386,51 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
           fr[c * cap + t] = 0.f;
         }
       }
-      gidx[t] = g;
       code[t] = (unsigned short)(lx | (ly << 5) | (lz << 10));
     }
   }
+  if (tid == 0) *(int*)(red + 8 * nw) = 0;  // work-unit counter
   __syncthreads();
 
-  const TileView TV{EX, EY, EZ, tx, ty, tz, lstart, ox, oy, oz, pf, code, slut, srows, A.lj.prune2, FP64};
   const LJ32 q32 = A.lj.p32[0];
   const LJ64 q64 = A.lj.p64[0];
   const float rcpre = A.lj.rc2max * 1.0001f + 1e-4f;  // FP32 prefilter of the FP64 form
   double esum = 0.0, wsum = 0.0;  // FP64 form
-  KSum ek, wk;                    // mixed form: Kahan merge of per-pass FP32 sums
+  FixSum ek, wk;                  // mixed form: exact fixed-point sums of FP32 terms
   int ncand = 0, neval = 0, nacc = 0;
   // per-warp item buffer: int4 (i | r << 16, lo1, lo2, n1 | n2 << 16)
   int4* items = (int4*)(smem + L.items) + warp * kItems;
+  // per-warp queue of accepted pairs (mixed form)
+  float4* qd = (float4*)(smem + L.queue) + warp * kItems;
+  int* qk = (int*)(smem + L.queue + 16 * kItems * nw) + warp * kItems;
+  int qn = 0;
   const unsigned lt = (1u << lane) - 1u;
-  const int nch = (total + 31) >> 5;
-  const int nunits = kRows * nch;
   int nbuf = 0;
 
-  for (int u = warp;; u += nw) {
-    const bool more = u < nunits;
-    if (more) {  // unit (r, chunk): items of 32 consecutive staged atoms for row r
-      const int r = u / nch, i = (u - r * nch) * 32 + lane;
-      int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
-      if (i < total) make_item(TV, i, r, lo1, n1, lo2, n2, COUNT ? &ncand : nullptr);
-      const unsigned b = __ballot_sync(FULL, n1 > 0);
-      if (n1 > 0) items[nbuf + __popc(b & lt)] = make_int4(i | (r << 16), lo1, lo2, n1 | (n2 << 16));
-      nbuf += __popc(b);
+  // ---- one pass: one item per lane, each lane walks its own j-ranges ----
+  auto run_pass = [&]() {
+    if (nbuf > 32) {
+      // Put the 32 longest items first (4 length buckets, stable), so that a
+      // pass holds items of similar length and the short ones wait for more.
+      const int4 a = items[lane];
+      const bool hb = lane + 32 < nbuf;
+      const int4 bb = hb ? items[lane + 32] : make_int4(0, 0, 0, 0);
+      const int na = (a.w & 0xffff) + (a.w >> 16), nb = hb ? (bb.w & 0xffff) + (bb.w >> 16) : -1;
+      const int ka = na >= 12 ? 0 : (na >= 7 ? 1 : (na >= 4 ? 2 : 3));
+      const int kb = !hb ? 4 : (nb >= 12 ? 0 : (nb >= 7 ? 1 : (nb >= 4 ? 2 : 3)));
+      int base = 0, pa = 0, pb = 0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const unsigned ba = __ballot_sync(FULL, ka == k), bbk = __ballot_sync(FULL, kb == k);
+        if (ka == k) pa = base + __popc(ba & lt);
+        if (kb == k) pb = base + __popc(ba) + __popc(bbk & lt);
+        base += __popc(ba) + __popc(bbk);
+      }
       __syncwarp();
-      if (nbuf < 32) continue;
-    } else if (nbuf == 0) {
-      break;
+      items[pa] = a;
+      if (hb) items[pb] = bb;
+      __syncwarp();
     }
-    // ---- one pass: one item per lane, each lane walks its own j-ranges ----
     const int cnt = min(nbuf, 32);
     int i = -1, r = 0, lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
     if (lane < cnt) {
@@ -399,38 +453,60 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
       const float Cx = -pi.x;
       const float Cy = dyt[ly * kDT + dy + 2] - pi.y;
       const float Cz = dzt[lz * kDT + dz + 2] - pi.z;
-      float ax = 0.f, ay = 0.f, az = 0.f, ea = 0.f, wa = 0.f;
-      for (int t = 0; t < tmax; ++t) {
-        if (t < nt) {
-          const int m = t < n1 ? lo1 + t : lo2 + (t - n1);
-          const float4 q = pf[m];
-          if (COUNT) ++neval;
-          const float dxv = q.x + Cx, dyv = q.y + Cy, dzv = q.z + Cz;
-          const float r2 = fmaf(dxv, dxv, fmaf(dyv, dyv, dzv * dzv));
-          LJ32 P = q32;
-          if (MULTI) P = A.lj.p32[ti * A.lj.nt + __float_as_int(q.w)];
-          if (r2 <= P.rc2) {
-            const float ri = rcp_approx(r2);
-            const float s2 = P.sig2 * ri;
-            const float s6 = s2 * s2 * s2;
-            const float dg = P.m24eps * s6 * fmaf(2.f, s6, -1.f) * ri;
-            ax = fmaf(dg, dxv, ax);
-            ay = fmaf(dg, dyv, ay);
-            az = fmaf(dg, dzv, az);
-            add_fixed(fa, fr, cap, m, -dg * dxv, -dg * dyv, -dg * dzv, A.status);
-            if (ENERGY) {
-              ea = fmaf(P.c4eps * s6, s6 - 1.f, ea);
-              wa = fmaf(-dg, r2, wa);
-            }
+      // distance tests only; accepted pairs go to the warp's queue and their
+      // forces are computed in full batches of 32 (force_batch)
+      // Four candidates per lane per step, tested independently (the loop is
+      // bound by load and arithmetic latency, not by issue), then enqueued.
+      const int kbase = i | (ti << 28);
+      constexpr int U = 4;
+      for (int t = 0; t < tmax; t += U) {
+        float4 dq[U];
+        int mm[U], tj[U];
+        bool acc[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+          const int tt = t + k;
+          mm[k] = tt < n1 ? lo1 + tt : lo2 + (tt - n1);
+          acc[k] = tt < nt;
+          const float4 q = pf[acc[k] ? mm[k] : 0];
+          dq[k].x = q.x + Cx;
+          dq[k].y = q.y + Cy;
+          dq[k].z = q.z + Cz;
+          dq[k].w = fmaf(dq[k].x, dq[k].x, fmaf(dq[k].y, dq[k].y, dq[k].z * dq[k].z));
+          tj[k] = __float_as_int(q.w);
+        }
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+          if (COUNT && acc[k]) ++neval;
+          const float rc2 = MULTI ? A.lj.p32[ti * A.lj.nt + tj[k]].rc2 : q32.rc2;
+          acc[k] = acc[k] && dq[k].w <= rc2;
+          const unsigned b = __ballot_sync(FULL, acc[k]);
+          if (acc[k]) {
+            const int p = qn + __popc(b & lt);
+            qd[p] = dq[k];
+            qk[p] = kbase | (mm[k] << 14) | (tj[k] << 30);
             if (COUNT) ++nacc;
           }
-        }
-      }
-      if (nt > 0) {
-        add_fixed(fa, fr, cap, i, ax, ay, az, A.status);
-        if (ENERGY) {
-          ek.add(ea);
-          wk.add(wa);
+          qn += __popc(b);
+          if (qn >= 32) {
+            __syncwarp();
+            force_batch<MULTI, ENERGY>(32, qd, qk, fa, fr, cap, A.lj, ek, wk);
+            __syncwarp();
+            const int rem = qn - 32;
+            float4 kd = make_float4(0.f, 0.f, 0.f, 0.f);
+            int kk = 0;
+            if (lane < rem) {
+              kd = qd[32 + lane];
+              kk = qk[32 + lane];
+            }
+            __syncwarp();
+            if (lane < rem) {
+              qd[lane] = kd;
+              qk[lane] = kk;
+            }
+            qn = rem;
+            __syncwarp();
+          }
         }
       }
     } else {
@@ -505,6 +581,95 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
     if (lane < rem) items[lane] = keep;
     nbuf = rem;
     __syncwarp();
+  };
+
+  // ---- work units: 32 consecutive staged atoms x one of four row groups ----
+  // Per-atom quantities that do not depend on the row (cell, position class,
+  // tile-frame position, x-distances to the neighbouring cells) are computed
+  // once per unit; each row then costs a mask lookup and the y/z distances.
+  const int nch = (total + 31) >> 5;
+  // Units are handed out by a shared counter: their cost varies a lot (halo
+  // atoms own few pairs), and the force sums do not depend on the order.
+  const int nunits = 4 * nch;
+  const float prune2 = A.lj.prune2;
+  int* ucnt = (int*)(red + 8 * nw);
+  while (true) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(ucnt, 1);
+    u = __shfl_sync(FULL, u, 0);
+    if (u >= nunits) break;
+    const int c = u >> 2, g = u & 3;
+    const int r0 = 3 * g, r1 = g == 3 ? kRows : 3 * g + 3;
+    const int i = c * 32 + lane;
+    const bool vi = i < total;
+    const int ci = code[vi ? i : 0];
+    const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
+    const unsigned char* lrow =
+        slut + (pos_class(lx - 1, tx) * 25 + pos_class(ly - 1, ty) * 5 + pos_class(lz - 1, tz)) * kRows;
+    const float4 pi = pf[vi ? i : 0];
+    const float py = FP64 ? pi.y : oy[ly] + pi.y;
+    const float pz = FP64 ? pi.z : oz[lz] + pi.z;
+    // squared x-gaps to the cells dx = -2, -1, +1, +2 (tile frame; ox has EX+1 entries)
+    const float gm2 = fmaxf(pi.x - ox[max(lx - 1, 0)], 0.f), gm1 = fmaxf(pi.x - ox[lx], 0.f);
+    const float gp1 = fmaxf(ox[min(lx + 1, EX)] - pi.x, 0.f), gp2 = fmaxf(ox[min(lx + 2, EX)] - pi.x, 0.f);
+    const float gx2[5] = {gm2 * gm2, gm1 * gm1, 0.f, gp1 * gp1, gp2 * gp2};
+    for (int r = r0; r < r1; ++r) {
+      int mask = vi ? lrow[r] : 0;
+      int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
+      if (mask) {
+        const int dy = srows[2 * r], dz = srows[2 * r + 1];
+        const int rowbase = ((ly + dy) + EY * (lz + dz)) * EX + lx - 2;  // + bit b -> ext cell of dx = b - 2
+        if (COUNT) {  // every atom of the owned cells, as the reference visits them
+          for (int b = 0; b < 5; ++b)
+            if ((mask >> b) & 1) {
+              const int e = rowbase + b;
+              ncand += (r == kRows - 1 && b == 2) ? lstart[e + 1] - i - 1 : lstart[e + 1] - lstart[e];
+            }
+        }
+        // distance from the atom to the cell boxes (the 1e-4 margin in
+        // prune2 covers the FP32 rounding)
+        const float gy = dy > 0 ? oy[ly + dy] - py : (dy < 0 ? py - oy[ly + dy + 1] : 0.f);
+        const float gz = dz > 0 ? oz[lz + dz] - pz : (dz < 0 ? pz - oz[lz + dz + 1] : 0.f);
+        const float g2 = fmaxf(gy, 0.f) * fmaxf(gy, 0.f) + fmaxf(gz, 0.f) * fmaxf(gz, 0.f);
+        if (g2 > prune2) mask = 0;
+#pragma unroll
+        for (int b = 0; b < 5; ++b)
+          if (b != 2 && gx2[b] + g2 > prune2) mask &= ~(1 << b);
+        if (mask) {
+          const int b0 = __ffs(mask) - 1;
+          int b1 = b0;
+          while (b1 < 4 && ((mask >> (b1 + 1)) & 1)) ++b1;
+          lo1 = lstart[rowbase + b0];
+          n1 = lstart[rowbase + b1 + 1] - lo1;
+          if (r == kRows - 1 && b0 == 2) {  // pairs inside A: a2 > a1
+            n1 -= i + 1 - lo1;
+            lo1 = i + 1;
+          }
+          const int m2 = mask & ~((2 << b1) - 1);
+          if (m2) {
+            const int c0b = __ffs(m2) - 1, c1b = 31 - __clz(m2);
+            lo2 = lstart[rowbase + c0b];
+            n2 = lstart[rowbase + c1b + 1] - lo2;
+          }
+          if (n1 <= 0) {
+            lo1 = lo2;
+            n1 = n2;
+            lo2 = 0;
+            n2 = 0;
+          }
+        }
+      }
+      const unsigned b = __ballot_sync(FULL, n1 > 0);
+      if (n1 > 0) items[nbuf + __popc(b & lt)] = make_int4(i | (r << 16), lo1, lo2, n1 | (max(n2, 0) << 16));
+      nbuf += __popc(b);
+      __syncwarp();
+      if (nbuf >= 32) run_pass();
+    }
+  }
+  while (nbuf > 0) run_pass();
+  if (!FP64 && qn > 0) {  // the last, partial batch
+    __syncwarp();
+    force_batch<MULTI, ENERGY>(qn, qd, qk, fa, fr, cap, A.lj, ek, wk);
   }
   __syncthreads();
 
@@ -514,7 +679,8 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
     const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
     const int slot = ((lx == 0 || lx == EX - 1) ? 1 : 0) | ((ly == 0 || ly == EY - 1) ? 2 : 0) |
                      ((lz == 0 || lz == EZ - 1) ? 4 : 0);
-    const int64_t g = gidx[t];
+    const int e = lx + EX * (ly + EY * lz);
+    const int64_t g = gfirst[e] + (t - lstart[e]);
     if (FP64) {
       double* F = slot == 0 ? (double*)A.Fown : (double*)A.P + (size_t)(slot - 1) * 3 * A.N;
 #pragma unroll
@@ -530,53 +696,59 @@ __global__ void __launch_bounds__(256) k_pair(const PairArgs A) {
 
   // (5) per-tile energy / virial / counters
   if (ENERGY || COUNT) {
+    // mixed form: exact integer sums (the same bits whatever the order);
+    // FP64 form: FP64 sums
     double e = 0.0, w = 0.0;
+    long long ev = 0, wv = 0;
     if (ENERGY) {
       if (FP64) {
         e = esum;
         w = wsum;
       } else {
-        e = (double)ek.s - (double)ek.c;
-        w = (double)wk.s - (double)wk.c;
+        ev = ek.v;
+        wv = wk.v;
+        e = (double)ek.side;
+        w = (double)wk.side;
       }
     }
     e = warp_sum(e);
     w = warp_sum(w);
+    ev = warp_sum(ev);
+    wv = warp_sum(wv);
     const long long c1 = warp_sum((long long)ncand), c2 = warp_sum((long long)nacc),
                     c3 = warp_sum((long long)neval);
+    long long* redl = (long long*)red;
     __syncthreads();
     if (lane == 0) {
-      red[4 * warp] = e;
-      red[4 * warp + 1] = w;
-      red[4 * warp + 2] = (double)c1;
-      red[4 * warp + 3] = (double)c2;
+      red[8 * warp] = e;
+      red[8 * warp + 1] = w;
+      redl[8 * warp + 2] = ev;
+      redl[8 * warp + 3] = wv;
+      redl[8 * warp + 4] = c1;
+      redl[8 * warp + 5] = c2;
+      redl[8 * warp + 6] = c3;
     }
     __syncthreads();
     if (tid == 0) {
-      double se = 0, sw = 0, s1 = 0, s2 = 0;
+      double se = 0, sw = 0;
+      long long sev = 0, swv = 0, s1 = 0, s2 = 0, s3 = 0;
       for (int k = 0; k < nw; ++k) {
-        se += red[4 * k];
-        sw += red[4 * k + 1];
-        s1 += red[4 * k + 2];
-        s2 += red[4 * k + 3];
+        se += red[8 * k];
+        sw += red[8 * k + 1];
+        sev += redl[8 * k + 2];
+        swv += redl[8 * k + 3];
+        s1 += redl[8 * k + 4];
+        s2 += redl[8 * k + 5];
+        s3 += redl[8 * k + 6];
       }
       if (ENERGY) {
-        A.tileE[tile] = se;
-        A.tileW[tile] = sw;
+        A.tileE[tile] = (double)sev * 0x1.0p-32 + se;
+        A.tileW[tile] = (double)swv * 0x1.0p-32 + sw;
       }
       if (COUNT) {
-        A.tileC[3 * tile] = (long long)s1;
-        A.tileC[3 * tile + 1] = (long long)s2;
-      }
-    }
-    if (COUNT) {
-      __syncthreads();
-      if (lane == 0) red[warp] = (double)c3;
-      __syncthreads();
-      if (tid == 0) {
-        double s3 = 0;
-        for (int k = 0; k < nw; ++k) s3 += red[k];
-        A.tileC[3 * tile + 2] = (long long)s3;
+        A.tileC[3 * tile] = s1;
+        A.tileC[3 * tile + 1] = s2;
+        A.tileC[3 * tile + 2] = s3;
       }
     }
   }
