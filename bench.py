@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 NC, RHO, RC, DT, T_MELT = 64, 0.8442, 2.5, 0.005, 1.0
 WORKLOAD = "lj-liquid-fcc64-1048576-rc2.5"
 METRIC = "atom-steps/s on 1 GB300: mixed-FP32 vs FP64 path at <=1e-5 RMS force rel. error"
-FP32_PEAK_TFLOPS = 73.6  # FFMA probe on this machine's GB300 (profiles/gb300_pipe_rates.txt)
+FP32_PEAK_TFLOPS = 73.84  # FFMA probe (python -m examd_gb300.peaks) on a GB300; used if the live probe fails
 
 
 def dist_info():
@@ -144,6 +144,18 @@ def read_traffic():
     return float(m.group(1)) if m else None
 
 
+def fp32_peak():
+    """FP32 FMA peak in TFLOP/s, measured now on this GPU by the pipe-rate probe."""
+    try:
+        from examd_gb300 import peaks
+        r = peaks.measure()
+        return float(r["fp32_tflops"]), (f"of measured: FFMA issue rate {r['ffma_per_clk_sm']:.1f}/clk/SM at "
+                                          f"{r['clock_mhz']:.0f} MHz, python -m examd_gb300.peaks, this run "
+                                          "(the driver-measured peaks have no FP32 figure)")
+    except Exception as e:  # the probe is a measurement aid; the committed figure stands in
+        return FP32_PEAK_TFLOPS, f"of measured earlier (profiles/gb300_pipe_rates.txt); live probe failed: {e}"
+
+
 def drift_per_1000(e):
     """Least-squares slope of (E - E0)/|E0| per 1000 steps."""
     e = np.asarray(e, dtype=np.float64)
@@ -241,6 +253,7 @@ def main():
     # pair-kernel roofline: algorithmic FLOPs per launch / event-timed duration
     cnt = sysm.counters()
     flops = 8.0 * cnt["candidates"] + 22.0 * cnt["accepted"]
+    peak, peak_src = fp32_peak()
     reps = 20
     _, k_ms = sysm.time_forces(reps)
     achieved = flops / (k_ms * 1e-3) / 1e12
@@ -294,10 +307,10 @@ def main():
             "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n},
             "gpu_launches": 7 * args.steps + 1,
             "roofline": {"bound": "fp32", "kernel": "k_pair (mixed)", "achieved": achieved,
-                         "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_TFLOPS,
+                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "traffic": traffic, "kernel_ms": k_ms, "flops_per_launch": flops,
                          "candidates": cnt["candidates"], "accepted": cnt["accepted"],
-                         "peak_source": "of measured FFMA rate (probe), MEASURED_PEAKS.json has no FP32 figure"},
+                         "peak_source": peak_src},
             **extra}
     if rk == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(melted, L)
