@@ -13,6 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libexamd_gb300.so")
 
 MAX_TYPES = 4
+STATIC_MAX_ATOMS = 1048576  # EXAMD_STATIC_MAX_ATOMS
+STATIC_MAX_BOXES = 4096     # EXAMD_STATIC_MAX_BOXES
 FP64 = 0
 MIXED = 1
 
@@ -84,6 +86,8 @@ def load():
             "examd_gpu_run": (C.c_int, [ctxp, C.c_int, C.c_double, C.c_int, dp, C.POINTER(Stats)]),
             "examd_gpu_get_state": (C.c_int, [ctxp, dp, dp]),
             "examd_gpu_kinetic": (C.c_int, [ctxp, dp]),
+            "examd_kinetic_static": (C.c_int, [C.c_int, C.c_int64, C.c_int, i64p, vp, vp, vp, vp, C.c_int, dp, dp,
+                                               vp, C.c_char_p, C.c_int]),
             "examd_gpu_scale_velocities": (C.c_int, [ctxp, dp]),
             "examd_gpu_time_forces": (C.c_int, [ctxp, C.c_int, dp, dp]),
             "examd_gpu_counters": (C.c_int, [ctxp, i64p, i64p, i64p, i64p, i64p]),

@@ -134,6 +134,33 @@ int examd_gpu_get_state(examd_ctx *ctx, double *pos, double *vel);
 /* Per-box kinetic energy (sum m v^2 / 2) at the current velocities. */
 int examd_gpu_kinetic(examd_ctx *ctx, double *ekin);
 
+/* Per-box kinetic energy of atoms in the CALLER's device arrays, with no
+ * device allocation (no counterpart in the reference, which has no device
+ * memory).  For callers that own their device memory and cannot let a library
+ * allocate between steps: a host MD code whose CUDA Fortran / OpenACC arrays or
+ * pool allocator hold the free HBM, where cudaMalloc can fail or fragment the
+ * pool and cudaFree would synchronise the device under the caller's streams.
+ * Scratch is one fixed static device array per device, so:
+ *   - natoms <= EXAMD_STATIC_MAX_ATOMS and 1 <= nboxes <= EXAMD_STATIC_MAX_BOXES,
+ *     else EXAMD_ERR_ARG before any device work;
+ *   - every call shares that array: calls whose device work overlaps (other
+ *     threads, or unordered streams) race; sequential calls are safe;
+ *   - the first call on a device sets up the array's address
+ *     (cudaGetSymbolAddress); make it before any stream capture begins.
+ * atom0: host, nboxes+1 offsets (0 .. natoms) of each box's contiguous atoms.
+ * vx, vy, vz: device, natoms doubles each.  type: device, natoms ints in
+ * [0, ntypes), or NULL for all type 0.  mass: host, ntypes doubles.  ekin:
+ * host, nboxes doubles.  stream: a cudaStream_t, or NULL for the default
+ * stream; the call synchronises it before returning.  errbuf (may be NULL):
+ * receives a one-line reason when the status is not EXAMD_OK. */
+#define EXAMD_STATIC_MAX_ATOMS 1048576
+#define EXAMD_STATIC_MAX_BOXES 4096
+int examd_kinetic_static(int device, int64_t natoms, int nboxes,
+                         const int64_t *atom0, const double *vx,
+                         const double *vy, const double *vz, const int *type,
+                         int ntypes, const double *mass, double *ekin,
+                         void *stream, char *errbuf, int errbuf_len);
+
 /* Scale all velocities of box b by factor[b] (thermostat / melt protocol). */
 int examd_gpu_scale_velocities(examd_ctx *ctx, const double *factor);
 
