@@ -93,7 +93,6 @@ bool build_own_lut(OwnLut& L) {
           }
           if (r == kRows - 1 && class_ok(cx, 0) && class_ok(cy, 0) && class_ok(cz, 0)) mask |= 1u << 2;
           L.lut[cls][r] = (unsigned char)mask;
-          if (mask) L.rowact[cy * 5 + cz] |= (unsigned short)(1u << r);
         }
       }
   return true;
@@ -434,14 +433,17 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     }
     B.bl = bl;
     B.bli = 1.0 / bl;
+    for (int a = 0; a < 3; ++a) B.remf[a] = (float)(B.L[a] - B.nb[a] * bl);  // nb*bl is exact
     B.blf = (float)bl;
     B.blif = (float)(1.0 / bl);
     B.cell0 = cell0;
     B.tile0 = (int)tiles.size() / 2;
     int starts[3][1025];
     for (int a = 0; a < 3; ++a) {
-      // tiles of about T cells (nearest count); every tile keeps >= 2 cells
-      B.nt[a] = std::max(1, std::min(B.nb[a] / 2, (2 * B.nb[a] + T[a]) / (2 * T[a])));
+      // tiles of at most T cells (T or T - 1 when nb is not a multiple), so the
+      // largest staged tile, which sizes shared memory, stays (T + 2)^3 cells;
+      // every tile keeps >= 2 cells
+      B.nt[a] = std::max(1, std::min(B.nb[a] / 2, (B.nb[a] + T[a] - 1) / T[a]));
       for (int k = 0; k <= B.nt[a]; ++k) starts[a][k] = (int)((int64_t)k * B.nb[a] / B.nt[a]);
       for (int k = 0; k < B.nt[a]; ++k)
         if (starts[a][k + 1] - starts[a][k] + 2 > kMaxExt) {

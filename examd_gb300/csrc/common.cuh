@@ -38,6 +38,7 @@ struct BoxDev {
   double L[3], Li[3];
   double bl, bli;  // block_length (cell edge) and its inverse
   float blf, blif, Lf[3];
+  float remf[3];   // L - nb*bl: the extra width of the last cell, FP32
   int nb[3];
   int cell0;       // first global cell id of the box
   int tile0;       // first tile of the box
@@ -67,12 +68,10 @@ struct LJTable {
 //   c_lut[cls][r] = 5-bit mask over dx = -2..2 of the cell pairs (A, A+d)
 //   owned by the tile when A's position class is cls.  Row 12 uses bit 2 for
 //   the pairs inside A (a1 < a2) and bits 3, 4 for dx = +1, +2.
-struct OwnLut {
-  signed char rows[kRows][2];
+// 16-byte aligned so that a CTA copies it to shared memory as uint4 words.
+struct __align__(16) OwnLut {
   unsigned char lut[kClasses][kRows];
-  // rowact[cy*5+cz] bit r: some x-class of a row with y/z classes (cy, cz)
-  // owns a pair in row r (lets a warp skip whole rows)
-  unsigned short rowact[25];
+  signed char rows[kRows][2];
 };
 
 __host__ __device__ inline int pos_class(int l, int t) {

@@ -16,9 +16,11 @@
 // of row r that the table assigns to this tile (ownership masks per position
 // class), trimmed to the cells whose box comes within rc of the atom (the
 // accepted pairs are unchanged).  Atoms without work are dropped and the items
-// are compacted into passes of 32 lanes.  A lane walks its own j-ranges: the
-// i-side partial sum stays in registers, the j-side terms (Newton's third
-// law) are added as they come.
+// are compacted into passes of up to 32 items.  Mixed form: the items'
+// candidate pairs are laid end to end and tested 32 at a time, one per lane;
+// accepted pairs are queued and their forces computed in batches of 32, both
+// atoms' sums updated (Newton's third law).  FP64 form: a lane walks its own
+// item's j-ranges with the i-side sum in registers.
 //
 // Accumulation.  Mixed form: each per-atom force component is an exact 32-bit
 // fixed-point sum in shared memory (scale 2^15, native integer atomics), so
@@ -50,7 +52,7 @@ constexpr float kFixMax = 1024.f;      // larger terms take the FP32 side path
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
-  int lstart, gfirst, ox, oy, oz, dyt, dzt, imx, imy, imz, red, lut, rows, items, queue;
+  int lstart, gfirst, ox, oy, oz, dyt, dzt, imx, imy, imz, red, lut, items, queue;
   int pf, fa, fr, px, code;
   int bytes;
 };
@@ -71,10 +73,9 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.imy = o;    o = align16(o + 8 * kMaxExt);
   L.imz = o;    o = align16(o + 8 * kMaxExt);
   L.red = o;    o = align16(o + 8 * 8 * nw + 16);  // + the CTA's unit counter
-  L.lut = o;    o = align16(o + kClasses * kRows);
-  L.rows = o;   o = align16(o + 2 * kRows);
+  L.lut = o;    o = align16(o + (int)sizeof(OwnLut));
   L.items = o;  o = align16(o + 16 * kItems * nw);
-  L.queue = o;  o = align16(o + (fp64 ? 0 : 20 * kItems * nw));
+  L.queue = o;  o = align16(o + (fp64 ? 0 : (20 * kItems + 16 * 32) * nw));  // + per-pass item table
   L.pf = o;     o = align16(o + 16 * cap);
   if (fp64) {
     L.fa = o;   o = align16(o + 3 * 8 * cap);  // FP64 force sums
@@ -94,79 +95,6 @@ int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max) {
   return make_layout(cfg.fp64, cap, ne_max, cfg.warps).bytes;
 }
 int pair_bytes_per_atom(const PairConfig& cfg) { return make_layout(cfg.fp64, 1024, 0, 1).bytes / 1024; }
-
-// Tile geometry and shared tables seen by the item builder.
-struct TileView {
-  int EX, EY, EZ, tx, ty, tz;
-  const int* lstart;
-  const float *ox, *oy, *oz;
-  const float4* pf;
-  const unsigned short* code;
-  const unsigned char* lut;
-  const signed char* rows;
-  float prune2;
-  bool fp64;
-};
-
-// j-ranges of atom i for row r: [lo1, lo1+n1) and [lo2, lo2+n2) in staged
-// order.  ncand (COUNT) gets the reference's candidate count of the item.
-__device__ __forceinline__ void make_item(const TileView& T, int i, int r, int& lo1, int& n1, int& lo2, int& n2,
-                                          int* ncand) {
-  lo1 = n1 = lo2 = n2 = 0;
-  const int ci = T.code[i];
-  const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
-  int mask = T.lut[(pos_class(lx - 1, T.tx) * 25 + pos_class(ly - 1, T.ty) * 5 + pos_class(lz - 1, T.tz)) * kRows + r];
-  if (!mask) return;
-  const int dy = T.rows[2 * r], dz = T.rows[2 * r + 1];
-  const int rowbase = ((ly + dy) + T.EY * (lz + dz)) * T.EX + lx - 2;  // + bit b -> ext cell of dx = b - 2
-  if (ncand) {  // every atom of the owned cells, as the reference visits them
-    for (int b = 0; b < 5; ++b)
-      if ((mask >> b) & 1) {
-        const int e = rowbase + b;
-        *ncand += (r == kRows - 1 && b == 2) ? T.lstart[e + 1] - i - 1 : T.lstart[e + 1] - T.lstart[e];
-      }
-  }
-  // distance from the atom to the cell boxes (tile frame, FP32; the 1e-4
-  // margin in prune2 covers the rounding)
-  const float4 pi = T.pf[i];
-  const float py = T.fp64 ? pi.y : T.oy[ly] + pi.y;
-  const float pz = T.fp64 ? pi.z : T.oz[lz] + pi.z;
-  const float gy = dy > 0 ? T.oy[ly + dy] - py : (dy < 0 ? py - T.oy[ly + dy + 1] : 0.f);
-  const float gz = dz > 0 ? T.oz[lz + dz] - pz : (dz < 0 ? pz - T.oz[lz + dz + 1] : 0.f);
-  const float g2 = fmaxf(gy, 0.f) * fmaxf(gy, 0.f) + fmaxf(gz, 0.f) * fmaxf(gz, 0.f);
-  if (g2 > T.prune2) return;
-#pragma unroll
-  for (int b = 0; b < 5; ++b) {
-    if (b == 2 || !((mask >> b) & 1)) continue;
-    const int dx = b - 2;
-    const float gx = dx > 0 ? T.ox[lx + dx] - pi.x : pi.x - T.ox[lx + dx + 1];
-    if (gx > 0.f && fmaf(gx, gx, g2) > T.prune2) mask &= ~(1 << b);
-  }
-  if (!mask) return;
-  const int b0 = __ffs(mask) - 1;
-  int b1 = b0;
-  while (b1 < 4 && ((mask >> (b1 + 1)) & 1)) ++b1;
-  lo1 = T.lstart[rowbase + b0];
-  n1 = T.lstart[rowbase + b1 + 1] - lo1;
-  if (r == kRows - 1 && b0 == 2) {  // pairs inside A: a2 > a1
-    n1 -= i + 1 - lo1;
-    lo1 = i + 1;
-  }
-  const int m2 = mask & ~((2 << b1) - 1);
-  if (m2) {
-    const int c0b = __ffs(m2) - 1, c1b = 31 - __clz(m2);
-    lo2 = T.lstart[rowbase + c0b];
-    n2 = T.lstart[rowbase + c1b + 1] - lo2;
-  }
-  if (n1 <= 0) {
-    lo1 = lo2;
-    n1 = n2;
-    lo2 = 0;
-    n2 = 0;
-  }
-  n1 = max(n1, 0);
-  n2 = max(n2, 0);
-}
 
 // Add a force term, given already multiplied by the fixed-point scale, to
 // atom m: exact fixed point, or the FP32 side path for a term too large for it.
@@ -239,7 +167,7 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
   const int X0 = t0.y, Y0 = t0.z, Z0 = t0.w;
   const int tx = t1.x, ty = t1.y, tz = t1.z;
   const int EX = tx + 2, EY = ty + 2, EZ = tz + 2;
-  const int NE = EX * EY * EZ, NR = EY * EZ;
+  const int NE = EX * EY * EZ;
   const Layout L = make_layout(FP64, A.cap, A.ne_max, nw);
   int* lstart = (int*)(smem + L.lstart);
   int* gfirst = (int*)(smem + L.gfirst);
@@ -252,8 +180,9 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
   double* imy = (double*)(smem + L.imy);
   double* imz = (double*)(smem + L.imz);
   double* red = (double*)(smem + L.red);
-  unsigned char* slut = (unsigned char*)(smem + L.lut);
-  signed char* srows = (signed char*)(smem + L.rows);
+  OwnLut* sown = (OwnLut*)(smem + L.lut);
+  const unsigned char* slut = &sown->lut[0][0];
+  const signed char* srows = &sown->rows[0][0];
   float4* pf = (float4*)(smem + L.pf);
   unsigned short* code = (unsigned short*)(smem + L.code);
   const int cap = A.cap;
@@ -273,13 +202,18 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
     gfirst[e] = s0;
     lstart[e] = A.cstart[gc + 1] - s0;
   }
-  for (int k = tid; k < kClasses * kRows; k += blockDim.x) slut[k] = c_own.lut[k / kRows][k % kRows];
-  if (tid < 2 * kRows) srows[tid] = c_own.rows[tid >> 1][tid & 1];
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(&c_own);
+    uint4* dst = reinterpret_cast<uint4*>(sown);
+    for (int k = tid; k < (int)(sizeof(OwnLut) / 16); k += blockDim.x) dst[k] = src[k];
+  }
   // Per-axis tables.  Ext coordinate l (cell X0 + l - 1, l = 0..E; l = E is
-  // the far edge of the last ext cell) has origin g*bl + n*L, g the wrapped
-  // cell and n its periodic image.  o*[l]: origin relative to the tile centre
-  // (FP32).  d*t[l*6 + d + 2]: exact origin difference between ext rows l and
-  // l + d rounded once (d = -2..3).  im*[l]: n*L (FP64).
+  // the far edge of the last ext cell) has origin (g0 + l - 1)*bl + n*r, with
+  // n = -1, 0, +1 its periodic image and r = L - nb*bl the extra width of the
+  // box's last cell.  o*[l]: origin relative to the tile centre, FP32 (the
+  // multiple of bl is exact, so the value is rounded once).  d*t[l*6 + d + 2]:
+  // origin difference between ext rows l and l + d (d = -2..3), rounded once.
+  // im*[l] (FP64 form): n*L.
   {
     const int a = tid >> 5, l = tid & 31;
     if (a < 3) {
@@ -287,25 +221,22 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
       const int g0 = a == 0 ? X0 : (a == 1 ? Y0 : Z0);
       const int t = a == 0 ? tx : (a == 1 ? ty : tz);
       const int nb = B.nb[a];
-      auto origin = [&](int ll) {
-        int g = g0 + ll - 1, n = 0;
-        if (g < 0) { g += nb; n = -1; }
-        if (g >= nb) { g -= nb; n = 1; }
-        return (double)((float)g * B.blf) + n * B.L[a];
+      const float blf = B.blf, rf = B.remf[a];
+      auto nimg = [&](int ll) {
+        const int g = g0 + ll - 1;
+        return g < 0 ? -1 : (g >= nb ? 1 : 0);
       };
       if (l <= E) {
-        const double org = origin(l);
-        const double centre = (double)((float)g0 * B.blf) + 0.5 * t * B.bl;
-        (a == 0 ? ox : (a == 1 ? oy : oz))[l] = (float)(org - centre);
+        const int n = nimg(l);
+        (a == 0 ? ox : (a == 1 ? oy : oz))[l] = fmaf((float)(2 * (l - 1) - t), 0.5f * blf, (float)n * rf);
         if (l < E) {
-          int g = g0 + l - 1;
-          (a == 0 ? imx : (a == 1 ? imy : imz))[l] = g < 0 ? -B.L[a] : (g >= nb ? B.L[a] : 0.0);
+          if (FP64) (a == 0 ? imx : (a == 1 ? imy : imz))[l] = n * B.L[a];
           if (a > 0) {
             float* dt = a == 1 ? dyt : dzt;
 #pragma unroll
             for (int d = -2; d <= 3; ++d) {
               const int l2 = l + d;
-              dt[l * kDT + d + 2] = (l2 >= 0 && l2 <= E) ? (float)(origin(l2) - org) : 0.f;
+              dt[l * kDT + d + 2] = (l2 >= 0 && l2 <= E) ? fmaf((float)(nimg(l2) - n), rf, (float)d * blf) : 0.f;
             }
           }
         }
@@ -356,20 +287,17 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
     }
     return;
   }
-  // (3) stage atoms row by row (a row of ext cells is contiguous in HBM
-  // unless it wraps)
+  // (3) stage atoms, one thread per ext cell
   int* fa = (int*)(smem + L.fa);
   float* fr = (float*)(smem + L.fr);
   double* fd = (double*)(smem + L.fa);
   double* pd = (double*)(smem + L.px);
-  for (int R = warp; R < NR; R += nw) {
-    const int e0 = R * EX, a0 = lstart[e0], a1 = lstart[e0 + EX];
-    const int ly = R % EY, lz = R / EY;
-    for (int t = a0 + lane; t < a1; t += 32) {
-      int lx = 0;
-      for (int k = 1; k < EX; ++k) lx += (lstart[e0 + k] <= t);
-      const int e = e0 + lx;
-      const int g = gfirst[e] + (t - lstart[e]);
+  for (int e = tid; e < NE; e += blockDim.x) {
+    const int lx = e % EX, rr = e / EX, ly = rr % EY, lz = rr / EY;
+    const int a0 = lstart[e], a1 = lstart[e + 1], g0 = gfirst[e];
+    const unsigned short cc = (unsigned short)(lx | (ly << 5) | (lz << 10));
+    for (int t = a0; t < a1; ++t) {
+      const int g = g0 + (t - a0);
       const float4 u = A.U[g];
       if (FP64) {
         pf[t] = make_float4(ox[lx] + u.x, oy[ly] + u.y, oz[lz] + u.z, u.w);
@@ -386,7 +314,7 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
           fr[c * cap + t] = 0.f;
         }
       }
-      code[t] = (unsigned short)(lx | (ly << 5) | (lz << 10));
+      code[t] = cc;
     }
   }
   if (tid == 0) *(int*)(red + 8 * nw) = 0;  // work-unit counter
@@ -407,9 +335,19 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
   const unsigned lt = (1u << lane) - 1u;
   int nbuf = 0;
 
-  // ---- one pass: one item per lane, each lane walks its own j-ranges ----
+  // per-warp table of the items of one mixed-form pass: (C, key base) and
+  // (lo1, n1, lo2 - n1, first candidate index)
+  float4* ptA = (float4*)(smem + L.queue + 20 * kItems * nw) + warp * 32;
+  int4* ptB = items;
+
+  // ---- one pass over the first min(nbuf, 32) items ----
+  // Mixed form: the items' candidate pairs are laid end to end and the warp
+  // walks them 32 at a time, one pair per lane, so no lane idles while another
+  // finishes a long j-range.  A lane finds its item from the bitmask of the
+  // items that start in the current 32 candidates.  FP64 form: one item per
+  // lane, each lane walks its own j-ranges.
   auto run_pass = [&]() {
-    if (nbuf > 32) {
+    if (FP64 && nbuf > 32) {
       // Put the 32 longest items first (4 length buckets, stable), so that a
       // pass holds items of similar length and the short ones wait for more.
       const int4 a = items[lane];
@@ -443,70 +381,82 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
       n2 = it.w >> 16;
     }
     const int nt = n1 + n2;
-    const int tmax = warp_max(nt);
     const float4 pi = pf[i >= 0 ? i : 0];
     const int ci = code[i >= 0 ? i : 0];
     const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
     const int dy = srows[2 * r], dz = srows[2 * r + 1];
     const int ti = __float_as_int(pi.w);
     if (!FP64) {
-      const float Cx = -pi.x;
-      const float Cy = dyt[ly * kDT + dy + 2] - pi.y;
-      const float Cz = dzt[lz * kDT + dz + 2] - pi.z;
-      // distance tests only; accepted pairs go to the warp's queue and their
-      // forces are computed in full batches of 32 (force_batch)
-      // Four candidates per lane per step, tested independently (the loop is
-      // bound by load and arithmetic latency, not by issue), then enqueued.
-      const int kbase = i | (ti << 28);
-      constexpr int U = 4;
-      for (int t = 0; t < tmax; t += U) {
-        float4 dq[U];
-        int mm[U], tj[U];
-        bool acc[U];
+      // exclusive scan of the items' candidate counts
+      int incl = nt;
 #pragma unroll
-        for (int k = 0; k < U; ++k) {
-          const int tt = t + k;
-          mm[k] = tt < n1 ? lo1 + tt : lo2 + (tt - n1);
-          acc[k] = tt < nt;
-          const float4 q = pf[acc[k] ? mm[k] : 0];
-          dq[k].x = q.x + Cx;
-          dq[k].y = q.y + Cy;
-          dq[k].z = q.z + Cz;
-          dq[k].w = fmaf(dq[k].x, dq[k].x, fmaf(dq[k].y, dq[k].y, dq[k].z * dq[k].z));
-          tj[k] = __float_as_int(q.w);
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int s0 = incl - nt;
+      const int T = __shfl_sync(FULL, incl, 31);
+      __syncwarp();
+      if (lane < cnt) {
+        // the atom's position moved into the j-cells' frame: d = x_j + C
+        const float Cx = -pi.x;
+        const float Cy = dyt[ly * kDT + dy + 2] - pi.y;
+        const float Cz = dzt[lz * kDT + dz + 2] - pi.z;
+        ptA[lane] = make_float4(Cx, Cy, Cz, __int_as_float(i | (ti << 28)));
+        ptB[lane] = make_int4(lo1, n1, lo2 - n1, s0);
+      }
+      __syncwarp();
+      // distance tests; accepted pairs go to the warp's queue and their forces
+      // are computed in full batches of 32 (force_batch)
+      int qbase = 0;  // items that start before K
+      for (int K = 0; K < T; K += 32) {
+        const unsigned M =
+            __reduce_or_sync(FULL, (lane < cnt && (unsigned)(s0 - K) < 32u) ? 1u << (s0 - K) : 0u);
+        const int q = qbase + __popc(M & (FULL >> (31 - lane))) - 1;  // item 0 starts at 0, so q >= 0
+        qbase += __popc(M);
+        const int k = K + lane;
+        const bool valid = k < T;
+        const float4 a = ptA[q];
+        const int4 b = ptB[q];
+        const int mo = k - b.w;
+        const int m = mo < b.y ? b.x + mo : b.z + mo;
+        const float4 pj = pf[valid ? m : 0];
+        float4 dq;
+        dq.x = pj.x + a.x;
+        dq.y = pj.y + a.y;
+        dq.z = pj.z + a.z;
+        dq.w = fmaf(dq.x, dq.x, fmaf(dq.y, dq.y, dq.z * dq.z));
+        const int tj = __float_as_int(pj.w);
+        const int kb = __float_as_int(a.w);
+        if (COUNT && valid) ++neval;
+        const float rc2 = MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
+        const bool acc = valid && dq.w <= rc2;
+        const unsigned bal = __ballot_sync(FULL, acc);
+        if (acc) {
+          const int p = qn + __popc(bal & lt);
+          qd[p] = dq;
+          qk[p] = kb | (m << 14) | (tj << 30);
+          if (COUNT) ++nacc;
         }
-#pragma unroll
-        for (int k = 0; k < U; ++k) {
-          if (COUNT && acc[k]) ++neval;
-          const float rc2 = MULTI ? A.lj.p32[ti * A.lj.nt + tj[k]].rc2 : q32.rc2;
-          acc[k] = acc[k] && dq[k].w <= rc2;
-          const unsigned b = __ballot_sync(FULL, acc[k]);
-          if (acc[k]) {
-            const int p = qn + __popc(b & lt);
-            qd[p] = dq[k];
-            qk[p] = kbase | (mm[k] << 14) | (tj[k] << 30);
-            if (COUNT) ++nacc;
+        qn += __popc(bal);
+        if (qn >= 32) {
+          __syncwarp();
+          force_batch<MULTI, ENERGY>(32, qd, qk, fa, fr, cap, A.lj, ek, wk);
+          __syncwarp();
+          const int rem = qn - 32;
+          float4 kd = make_float4(0.f, 0.f, 0.f, 0.f);
+          int kk = 0;
+          if (lane < rem) {
+            kd = qd[32 + lane];
+            kk = qk[32 + lane];
           }
-          qn += __popc(b);
-          if (qn >= 32) {
-            __syncwarp();
-            force_batch<MULTI, ENERGY>(32, qd, qk, fa, fr, cap, A.lj, ek, wk);
-            __syncwarp();
-            const int rem = qn - 32;
-            float4 kd = make_float4(0.f, 0.f, 0.f, 0.f);
-            int kk = 0;
-            if (lane < rem) {
-              kd = qd[32 + lane];
-              kk = qk[32 + lane];
-            }
-            __syncwarp();
-            if (lane < rem) {
-              qd[lane] = kd;
-              qk[lane] = kk;
-            }
-            qn = rem;
-            __syncwarp();
+          __syncwarp();
+          if (lane < rem) {
+            qd[lane] = kd;
+            qk[lane] = kk;
           }
+          qn = rem;
+          __syncwarp();
         }
       }
     } else {
@@ -522,6 +472,7 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
         sz = imz[lzj] - imz[lz];
         sxi = imx[lx];
       }
+      const int tmax = warp_max(nt);
       double ax = 0, ay = 0, az = 0;
       for (int t = 0; t < tmax; ++t) {
         if (t < nt) {

@@ -23,7 +23,7 @@ def pos_class(l, t):
 
 
 def tiles_1d(nb, T):
-    nt = max(1, min(nb // 2, (2 * nb + T) // (2 * T)))  # the library's partition rule
+    nt = max(1, min(nb // 2, (nb + T - 1) // T))  # the library's partition rule
     st = [k * nb // nt for k in range(nt + 1)]
     return [(st[k], st[k + 1] - st[k]) for k in range(nt)]
 
