@@ -93,6 +93,7 @@ bool build_own_lut(OwnLut& L) {
           }
           if (r == kRows - 1 && class_ok(cx, 0) && class_ok(cy, 0) && class_ok(cz, 0)) mask |= 1u << 2;
           L.lut[cls][r] = (unsigned char)mask;
+          if (mask) L.rlist[cls][L.nrow[cls]++] = (unsigned char)r;
         }
       }
   return true;

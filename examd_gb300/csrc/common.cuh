@@ -70,8 +70,10 @@ struct LJTable {
 //   the pairs inside A (a1 < a2) and bits 3, 4 for dx = +1, +2.
 // 16-byte aligned so that a CTA copies it to shared memory as uint4 words.
 struct __align__(16) OwnLut {
-  unsigned char lut[kClasses][kRows];
-  signed char rows[kRows][2];
+  unsigned char lut[kClasses][kRows];     // dx mask per position class and row
+  signed char rows[kRows][2];             // (dy, dz) of row r
+  unsigned char nrow[kClasses];           // rows with a nonzero mask
+  unsigned char rlist[kClasses][kRows];   // those rows, ascending
 };
 
 __host__ __device__ inline int pos_class(int l, int t) {

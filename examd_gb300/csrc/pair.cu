@@ -10,12 +10,12 @@
 //
 // Work order.  The 62 non-self table entries are, per cell A, 12 full x-rows
 // of 5 cells (dy, dz fixed, dx = -2..2) plus the half row dx = +1, +2; with
-// the pairs inside A that makes 13 "rows" r.  The work units of a tile are
-// (row r, 32 consecutive staged atoms); unit u goes to warp u mod W.  A warp
-// turns each atom of a unit into an item: the contiguous j-ranges of the cells
-// of row r that the table assigns to this tile (ownership masks per position
-// class), trimmed to the cells whose box comes within rc of the atom (the
-// accepted pairs are unchanged).  Atoms without work are dropped and the items
+// the pairs inside A that makes 13 "rows" r.  A warp turns (staged atom,
+// row) pairs into items: the contiguous j-ranges of the cells of row r that
+// the table assigns to this tile (ownership masks per position class),
+// trimmed to the cells whose box comes within rc of the atom (the accepted
+// pairs are unchanged).  Only rows with a nonzero mask for the atom's class
+// are visited, 32 (atom, row) pairs per step whatever the atom; the items
 // are compacted into passes of up to 32 items.  Mixed form: the items'
 // candidate pairs are laid end to end and tested 32 at a time, one per lane;
 // accepted pairs are queued and their forces computed in batches of 32, both
@@ -52,7 +52,7 @@ constexpr float kFixMax = 1024.f;      // larger terms take the FP32 side path
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
-  int lstart, gfirst, ox, oy, oz, dyt, dzt, imx, imy, imz, red, lut, items, queue;
+  int lstart, gfirst, ox, oy, oz, dyt, dzt, imx, imy, imz, red, r2l, lut, items, queue;
   int pf, fa, fr, px, code;
   int bytes;
 };
@@ -73,6 +73,7 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.imy = o;    o = align16(o + 8 * kMaxExt);
   L.imz = o;    o = align16(o + 8 * kMaxExt);
   L.red = o;    o = align16(o + 8 * 8 * nw + 16);  // + the CTA's unit counter
+  L.r2l = o;    o = align16(o + 32 * nw);
   L.lut = o;    o = align16(o + (int)sizeof(OwnLut));
   L.items = o;  o = align16(o + 16 * kItems * nw);
   L.queue = o;  o = align16(o + (fp64 ? 0 : (20 * kItems + 16 * 32) * nw));  // + per-pass item table
@@ -157,7 +158,7 @@ __device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int
 }
 
 template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
-__global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
+__global__ void __launch_bounds__(256, FP64 ? 2 : 4) k_pair(const PairArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -534,38 +535,71 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
     __syncwarp();
   };
 
-  // ---- work units: 32 consecutive staged atoms x one of four row groups ----
-  // Per-atom quantities that do not depend on the row (cell, position class,
-  // tile-frame position, x-distances to the neighbouring cells) are computed
-  // once per unit; each row then costs a mask lookup and the y/z distances.
-  const int nch = (total + 31) >> 5;
-  // Units are handed out by a shared counter: their cost varies a lot (halo
-  // atoms own few pairs), and the force sums do not depend on the order.
-  const int nunits = 4 * nch;
+  // ---- item building: (staged atom, owned row) pairs, laid end to end ----
+  // A unit is 32 consecutive staged atoms and one half of each atom's list of
+  // owned rows (the rows whose ownership mask for the atom's position class is
+  // nonzero; ordinals n = 2m + half).  The warp lays the unit's (atom, row)
+  // pairs end to end and builds one item per lane per step, so lanes do not
+  // idle on atoms that own few rows (the halo).  Units are handed out by a
+  // shared counter: their cost varies, and the force sums do not depend on the
+  // order.  An item is the atom's j-range(s) in the row: the owned cells,
+  // trimmed to those whose box comes within rc of the atom (the 1e-4 margin in
+  // prune2 covers the FP32 rounding; the accepted pairs are unchanged).
+  const int nunits = 2 * ((total + 31) >> 5);
   const float prune2 = A.lj.prune2;
   int* ucnt = (int*)(red + 8 * nw);
+  unsigned char* r2l = smem + L.r2l + 32 * warp;  // rank among working lanes -> lane
   while (true) {
     int u = 0;
     if (lane == 0) u = atomicAdd(ucnt, 1);
     u = __shfl_sync(FULL, u, 0);
     if (u >= nunits) break;
-    const int c = u >> 2, g = u & 3;
-    const int r0 = 3 * g, r1 = g == 3 ? kRows : 3 * g + 3;
-    const int i = c * 32 + lane;
-    const bool vi = i < total;
-    const int ci = code[vi ? i : 0];
-    const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
-    const unsigned char* lrow =
-        slut + (pos_class(lx - 1, tx) * 25 + pos_class(ly - 1, ty) * 5 + pos_class(lz - 1, tz)) * kRows;
-    const float4 pi = pf[vi ? i : 0];
-    const float py = FP64 ? pi.y : oy[ly] + pi.y;
-    const float pz = FP64 ? pi.z : oz[lz] + pi.z;
-    // squared x-gaps to the cells dx = -2, -1, +1, +2 (tile frame; ox has EX+1 entries)
-    const float gm2 = fmaxf(pi.x - ox[max(lx - 1, 0)], 0.f), gm1 = fmaxf(pi.x - ox[lx], 0.f);
-    const float gp1 = fmaxf(ox[min(lx + 1, EX)] - pi.x, 0.f), gp2 = fmaxf(ox[min(lx + 2, EX)] - pi.x, 0.f);
-    const float gx2[5] = {gm2 * gm2, gm1 * gm1, 0.f, gp1 * gp1, gp2 * gp2};
-    for (int r = r0; r < r1; ++r) {
-      int mask = vi ? lrow[r] : 0;
+    const int c = u >> 1, half = u & 1;
+    // per-atom quantities of lane l's atom c*32 + l
+    const int ia = c * 32 + lane;
+    const bool va = ia < total;
+    const int cia = code[va ? ia : 0];
+    const int ax = cia & 31, ay = (cia >> 5) & 31, az = cia >> 10;
+    const int acls = pos_class(ax - 1, tx) * 25 + pos_class(ay - 1, ty) * 5 + pos_class(az - 1, tz);
+    const int aw = va ? (sown->nrow[acls] + 1 - half) >> 1 : 0;
+    const float4 pa = pf[va ? ia : 0];
+    const float apy = FP64 ? pa.y : oy[ay] + pa.y;  // tile-frame y, z
+    const float apz = FP64 ? pa.z : oz[az] + pa.z;
+    // squared x-gaps to the cells dx = -2, -1, +1, +2 (ox has EX + 1 entries)
+    const float gm2 = fmaxf(pa.x - ox[max(ax - 1, 0)], 0.f), gm1 = fmaxf(pa.x - ox[ax], 0.f);
+    const float gp1 = fmaxf(ox[min(ax + 1, EX)] - pa.x, 0.f), gp2 = fmaxf(ox[min(ax + 2, EX)] - pa.x, 0.f);
+    const float am2 = gm2 * gm2, am1 = gm1 * gm1, ap1 = gp1 * gp1, ap2 = gp2 * gp2;
+    int incl = aw;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int as0 = incl - aw, W = __shfl_sync(FULL, incl, 31);
+    const unsigned wb = __ballot_sync(FULL, aw > 0);
+    if (aw > 0) r2l[__popc(wb & lt)] = (unsigned char)lane;
+    __syncwarp();
+    int qb = 0;  // working atoms that start before K
+    for (int K = 0; K < W; K += 32) {
+      const unsigned M = __reduce_or_sync(FULL, (aw > 0 && (unsigned)(as0 - K) < 32u) ? 1u << (as0 - K) : 0u);
+      const int qr = qb + __popc(M & (FULL >> (31 - lane))) - 1;  // >= 0: the first worker starts at 0
+      qb += __popc(M);
+      const int k = K + lane;
+      const bool valid = k < W;
+      const int ql = r2l[qr];
+      const int s_q = __shfl_sync(FULL, as0, ql);
+      const int ci = __shfl_sync(FULL, cia, ql);
+      const int cls = __shfl_sync(FULL, acls, ql);
+      const float py = __shfl_sync(FULL, apy, ql), pz = __shfl_sync(FULL, apz, ql);
+      const float xm2 = __shfl_sync(FULL, am2, ql), xm1 = __shfl_sync(FULL, am1, ql);
+      const float xp1 = __shfl_sync(FULL, ap1, ql), xp2 = __shfl_sync(FULL, ap2, ql);
+      const int i = c * 32 + ql;
+      const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
+      int r = 0, mask = 0;
+      if (valid) {
+        r = sown->rlist[cls][2 * (k - s_q) + half];
+        mask = sown->lut[cls][r];
+      }
       int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
       if (mask) {
         const int dy = srows[2 * r], dz = srows[2 * r + 1];
@@ -577,30 +611,29 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
               ncand += (r == kRows - 1 && b == 2) ? lstart[e + 1] - i - 1 : lstart[e + 1] - lstart[e];
             }
         }
-        // distance from the atom to the cell boxes (the 1e-4 margin in
-        // prune2 covers the FP32 rounding)
+        // distance from the atom to the row's cell boxes
         const float gy = dy > 0 ? oy[ly + dy] - py : (dy < 0 ? py - oy[ly + dy + 1] : 0.f);
         const float gz = dz > 0 ? oz[lz + dz] - pz : (dz < 0 ? pz - oz[lz + dz + 1] : 0.f);
         const float g2 = fmaxf(gy, 0.f) * fmaxf(gy, 0.f) + fmaxf(gz, 0.f) * fmaxf(gz, 0.f);
-        if (g2 > prune2) mask = 0;
-#pragma unroll
-        for (int b = 0; b < 5; ++b)
-          if (b != 2 && gx2[b] + g2 > prune2) mask &= ~(1 << b);
+        const float tr = prune2 - g2;
+        if (tr < 0.f) mask = 0;
+        mask &= ~((xm2 > tr ? 1 : 0) | (xm1 > tr ? 2 : 0) | (xp1 > tr ? 8 : 0) | (xp2 > tr ? 16 : 0));
         if (mask) {
-          const int b0 = __ffs(mask) - 1;
-          int b1 = b0;
-          while (b1 < 4 && ((mask >> (b1 + 1)) & 1)) ++b1;
+          const int b0 = __ffs(mask) - 1, b1 = 31 - __clz(mask);
+          const int mm = mask >> b0;
           lo1 = lstart[rowbase + b0];
-          n1 = lstart[rowbase + b1 + 1] - lo1;
-          if (r == kRows - 1 && b0 == 2) {  // pairs inside A: a2 > a1
+          int hi1 = lstart[rowbase + b1 + 1];
+          if (mm & (mm + 1)) {  // two runs: [b0, e1) and [b2, b1]
+            const int e1 = b0 + __ffs(~mm) - 1;
+            const int b2 = __ffs(mask & ~((1 << e1) - 1)) - 1;
+            lo2 = lstart[rowbase + b2];
+            n2 = hi1 - lo2;
+            hi1 = lstart[rowbase + e1];
+          }
+          n1 = hi1 - lo1;
+          if (r == kRows - 1 && b0 == 2) {  // pairs inside the cell: a2 > a1
             n1 -= i + 1 - lo1;
             lo1 = i + 1;
-          }
-          const int m2 = mask & ~((2 << b1) - 1);
-          if (m2) {
-            const int c0b = __ffs(m2) - 1, c1b = 31 - __clz(m2);
-            lo2 = lstart[rowbase + c0b];
-            n2 = lstart[rowbase + c1b + 1] - lo2;
           }
           if (n1 <= 0) {
             lo1 = lo2;
@@ -611,11 +644,12 @@ __global__ void __launch_bounds__(256, 4) k_pair(const PairArgs A) {
         }
       }
       const unsigned b = __ballot_sync(FULL, n1 > 0);
-      if (n1 > 0) items[nbuf + __popc(b & lt)] = make_int4(i | (r << 16), lo1, lo2, n1 | (max(n2, 0) << 16));
+      if (n1 > 0) items[nbuf + __popc(b & lt)] = make_int4(i | (r << 16), lo1, lo2, n1 | (n2 << 16));
       nbuf += __popc(b);
       __syncwarp();
       if (nbuf >= 32) run_pass();
     }
+    __syncwarp();
   }
   while (nbuf > 0) run_pass();
   if (!FP64 && qn > 0) {  // the last, partial batch
