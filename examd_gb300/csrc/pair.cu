@@ -16,11 +16,11 @@
 // trimmed to the cells whose box comes within rc of the atom (the accepted
 // pairs are unchanged).  Only rows with a nonzero mask for the atom's class
 // are visited, 32 (atom, row) pairs per step whatever the atom; the items
-// are compacted into passes of up to 32 items.  Mixed form: the items'
-// candidate pairs are laid end to end and tested 32 at a time, one per lane;
-// accepted pairs are queued and their forces computed in batches of 32, both
-// atoms' sums updated (Newton's third law).  FP64 form: a lane walks its own
-// item's j-ranges with the i-side sum in registers.
+// of one step (at most 32) have their candidate pairs laid end to end and
+// tested 32 at a time, one per lane.  Accepted pairs are queued and their
+// forces computed in batches of 32, both atoms' sums updated (Newton's third
+// law).  The FP64 form tests the candidates with an FP32 prefilter on a
+// widened cutoff and computes the queued pairs in FP64.
 //
 // Accumulation.  Mixed form: each per-atom force component is an exact 32-bit
 // fixed-point sum in shared memory (scale 2^15, native integer atomics), so
@@ -45,14 +45,14 @@ __constant__ OwnLut c_own;
 cudaError_t upload_own_lut(const OwnLut& lut) { return cudaMemcpyToSymbol(c_own, &lut, sizeof(OwnLut)); }
 
 constexpr int kDT = 6;        // origin differences for d = -2..3
-constexpr int kItems = 64;    // per-warp item buffer
+constexpr int kQueue = 64;    // per-warp queue of accepted pairs
 constexpr float kFix = 32768.f;        // fixed-point scale 2^15
 constexpr float kFixInv = 1.f / 32768.f;
 constexpr float kFixMax = 1024.f;      // larger terms take the FP32 side path
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
-  int lstart, gfirst, ox, oy, oz, dyt, dzt, imx, imy, imz, red, r2l, lut, items, queue;
+  int lstart, gfirst, ox, oy, oz, dyt, dzt, img, red, r2l, lut, queue;
   int pf, fa, fr, px, code;
   int bytes;
 };
@@ -69,14 +69,11 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.oz = o;     o = align16(o + 4 * (kMaxExt + 1));
   L.dyt = o;    o = align16(o + 4 * kMaxExt * kDT);
   L.dzt = o;    o = align16(o + 4 * kMaxExt * kDT);
-  L.imx = o;    o = align16(o + 8 * kMaxExt);
-  L.imy = o;    o = align16(o + 8 * kMaxExt);
-  L.imz = o;    o = align16(o + 8 * kMaxExt);
+  L.img = o;    o = align16(o + (fp64 ? 3 * 32 : 0));  // periodic image per ext coordinate (FP64 form)
   L.red = o;    o = align16(o + 8 * 8 * nw + 16);  // + the CTA's unit counter
-  L.r2l = o;    o = align16(o + 32 * nw);
+  L.r2l = o;    o = align16(o + 64 * nw);
   L.lut = o;    o = align16(o + (int)sizeof(OwnLut));
-  L.items = o;  o = align16(o + 16 * kItems * nw);
-  L.queue = o;  o = align16(o + (fp64 ? 0 : (20 * kItems + 16 * 32) * nw));  // + per-pass item table
+  L.queue = o;  o = align16(o + ((fp64 ? 4 : 20) * kQueue + 16 * 32) * nw);  // + one step's item table
   L.pf = o;     o = align16(o + 16 * cap);
   if (fp64) {
     L.fa = o;   o = align16(o + 3 * 8 * cap);  // FP64 force sums
@@ -96,20 +93,6 @@ int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max) {
   return make_layout(cfg.fp64, cap, ne_max, cfg.warps).bytes;
 }
 int pair_bytes_per_atom(const PairConfig& cfg) { return make_layout(cfg.fp64, 1024, 0, 1).bytes / 1024; }
-
-// Add a force term, given already multiplied by the fixed-point scale, to
-// atom m: exact fixed point, or the FP32 side path for a term too large for it.
-__device__ __forceinline__ void add_fixed(int* fa, float* fr, int cap, int m, float fx, float fy, float fz) {
-  if (fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) < kFixMax * kFix) {
-    atomicAdd(&fa[m], __float2int_rn(fx));
-    atomicAdd(&fa[cap + m], __float2int_rn(fy));
-    atomicAdd(&fa[2 * cap + m], __float2int_rn(fz));
-  } else {
-    atomicAdd(&fr[m], fx * kFixInv);
-    atomicAdd(&fr[cap + m], fy * kFixInv);
-    atomicAdd(&fr[2 * cap + m], fz * kFixInv);
-  }
-}
 
 // Exact sum of FP32 terms in 64-bit fixed point (2^-32 resolution): the total
 // does not depend on the order of the terms.  A term of magnitude >= 30000
@@ -132,14 +115,24 @@ struct FixSum {
 // Forces of cnt queued accepted pairs, one per lane: entry = (d = x_j - x_i,
 // r^2) and key = i | j << 14 | type_i << 28 | type_j << 30.  user_func.f90:58-69
 // in FP32: dg = -24 eps (2 s^12 - s^6) / r^2, f_i += dg d, f_j -= dg d.
+// The queue keeps an atom's accepted pairs next to each other, so the i-side
+// fixed-point terms are first summed over each run of lanes with the same i
+// (a segmented shuffle scan; integer sums, so the result is exact) and the
+// run's last lane adds the total: one shared atomic per run instead of one
+// per pair on the same address.
 template <bool MULTI, bool ENERGY>
 __device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int* qk, int* fa, float* fr, int cap,
                                             const LJTable& lj, FixSum& ek, FixSum& wk) {
+  const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  if (lane < cnt) {
+  const bool act = lane < cnt;
+  int i = -1, m = 0;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  if (act) {
     const float4 d = qd[lane];
     const unsigned key = (unsigned)qk[lane];
-    const int i = key & 0x3fff, m = (key >> 14) & 0x3fff;
+    i = key & 0x3fff;
+    m = (key >> 14) & 0x3fff;
     LJ32 P = lj.p32[0];
     if (MULTI) P = lj.p32[((key >> 28) & 3) * lj.nt + (key >> 30)];
     const float ri = rcp_approx(d.w);
@@ -147,18 +140,104 @@ __device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int
     const float s6 = s2 * s2 * s2;
     const float dg = P.m24eps * s6 * fmaf(2.f, s6, -1.f) * ri;
     const float dgs = kFix * dg;
-    const float fx = dgs * d.x, fy = dgs * d.y, fz = dgs * d.z;
-    add_fixed(fa, fr, cap, i, fx, fy, fz);
-    add_fixed(fa, fr, cap, m, -fx, -fy, -fz);
+    fx = dgs * d.x;
+    fy = dgs * d.y;
+    fz = dgs * d.z;
     if (ENERGY) {
       ek.add(P.c4eps * s6 * (s6 - 1.f));
       wk.add(-dg * d.w);
     }
   }
+  // terms too large for the fixed-point sums take the FP32 side path
+  const bool big = act && fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) >= kFixMax * kFix;
+  int ix = 0, iy = 0, iz = 0;
+  if (act && !big) {
+    ix = __float2int_rn(fx);
+    iy = __float2int_rn(fy);
+    iz = __float2int_rn(fz);
+    atomicAdd(&fa[m], -ix);
+    atomicAdd(&fa[cap + m], -iy);
+    atomicAdd(&fa[2 * cap + m], -iz);
+  }
+  if (big) {
+    atomicAdd(&fr[i], fx * kFixInv);
+    atomicAdd(&fr[cap + i], fy * kFixInv);
+    atomicAdd(&fr[2 * cap + i], fz * kFixInv);
+    atomicAdd(&fr[m], -fx * kFixInv);
+    atomicAdd(&fr[cap + m], -fy * kFixInv);
+    atomicAdd(&fr[2 * cap + m], -fz * kFixInv);
+  }
+  // i side: sum over runs of equal i (inactive lanes form one run with i = -1)
+  const int ip = __shfl_up_sync(FULL, i, 1);
+  const unsigned hb = __ballot_sync(FULL, lane == 0 || ip != i);
+  const int dist = lane - (31 - __clz(hb & (FULL >> (31 - lane))));
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int yx = __shfl_up_sync(FULL, ix, o), yy = __shfl_up_sync(FULL, iy, o), yz = __shfl_up_sync(FULL, iz, o);
+    if (o <= dist) {
+      ix += yx;
+      iy += yy;
+      iz += yz;
+    }
+  }
+  const bool tail = lane == 31 || ((hb >> (lane + 1)) & 1u);
+  if (act && tail) {
+    atomicAdd(&fa[i], ix);
+    atomicAdd(&fa[cap + i], iy);
+    atomicAdd(&fa[2 * cap + i], iz);
+  }
+}
+
+// FP64 form: the reference's arithmetic for cnt queued pairs that passed the
+// FP32 prefilter, one per lane (key as in force_batch).  The separation is
+// x_j - x_i plus the difference of the two staged copies' periodic images,
+// (n_j - n_i) L, which is exact (Sterbenz) and equals the reference's
+// dx - Nint(dx/L) L (SRC/exaMD_forces.f90:509-523); then user_func.f90:52-69.
+template <bool MULTI, bool ENERGY, bool COUNT>
+__device__ __forceinline__ void force_batch64(int cnt, const int* qk, const double* pd, const unsigned short* code,
+                                              const signed char* img, const double* Lbox, double* fd, int cap,
+                                              const LJTable& lj, double& esum, double& wsum, int& nacc) {
+  const int lane = threadIdx.x & 31;
+  if (lane >= cnt) return;
+  const unsigned key = (unsigned)qk[lane];
+  const int i = key & 0x3fff, m = (key >> 14) & 0x3fff;
+  const int ci = code[i], cm = code[m];
+  // difference of the copies' periodic images per axis: -1, 0 or +1 box
+  const int nx = img[cm & 31] - img[ci & 31];
+  const int ny = img[32 + ((cm >> 5) & 31)] - img[32 + ((ci >> 5) & 31)];
+  const int nz = img[64 + (cm >> 10)] - img[64 + (ci >> 10)];
+  double dx = __dsub_rn(pd[m], pd[i]);
+  double dy = __dsub_rn(pd[cap + m], pd[cap + i]);
+  double dz = __dsub_rn(pd[2 * cap + m], pd[2 * cap + i]);
+  if (nx) dx = __dadd_rn(dx, nx > 0 ? Lbox[0] : -Lbox[0]);
+  if (ny) dy = __dadd_rn(dy, ny > 0 ? Lbox[1] : -Lbox[1]);
+  if (nz) dz = __dadd_rn(dz, nz > 0 ? Lbox[2] : -Lbox[2]);
+  const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  LJ64 P = lj.p64[0];
+  if (MULTI) P = lj.p64[((key >> 28) & 3) * lj.nt + (key >> 30)];
+  if (d2 <= P.rc2) {
+    const double d2i = __drcp_rn(d2);
+    const double tt = __dmul_rn(P.sig2, d2i);
+    const double d6 = __dmul_rn(__dmul_rn(tt, tt), tt);
+    const double d12 = __dmul_rn(d6, d6);
+    const double dg = -__dmul_rn(__dmul_rn(P.eps24, __dsub_rn(__dmul_rn(2.0, d12), d6)), d2i);
+    const double fx = __dmul_rn(dg, dx), fy = __dmul_rn(dg, dy), fz = __dmul_rn(dg, dz);
+    atomicAdd(&fd[i], fx);
+    atomicAdd(&fd[cap + i], fy);
+    atomicAdd(&fd[2 * cap + i], fz);
+    atomicAdd(&fd[m], -fx);
+    atomicAdd(&fd[cap + m], -fy);
+    atomicAdd(&fd[2 * cap + m], -fz);
+    if (ENERGY) {
+      esum += __dmul_rn(P.eps4, __dsub_rn(d12, d6));
+      wsum += -__dmul_rn(dg, d2);
+    }
+    if (COUNT) ++nacc;
+  }
 }
 
 template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
-__global__ void __launch_bounds__(256, FP64 ? 2 : 4) k_pair(const PairArgs A) {
+__global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -177,9 +256,7 @@ __global__ void __launch_bounds__(256, FP64 ? 2 : 4) k_pair(const PairArgs A) {
   float* oz = (float*)(smem + L.oz);
   float* dyt = (float*)(smem + L.dyt);
   float* dzt = (float*)(smem + L.dzt);
-  double* imx = (double*)(smem + L.imx);
-  double* imy = (double*)(smem + L.imy);
-  double* imz = (double*)(smem + L.imz);
+  signed char* img = (signed char*)(smem + L.img);
   double* red = (double*)(smem + L.red);
   OwnLut* sown = (OwnLut*)(smem + L.lut);
   const unsigned char* slut = &sown->lut[0][0];
@@ -214,7 +291,7 @@ __global__ void __launch_bounds__(256, FP64 ? 2 : 4) k_pair(const PairArgs A) {
   // box's last cell.  o*[l]: origin relative to the tile centre, FP32 (the
   // multiple of bl is exact, so the value is rounded once).  d*t[l*6 + d + 2]:
   // origin difference between ext rows l and l + d (d = -2..3), rounded once.
-  // im*[l] (FP64 form): n*L.
+  // img[32a + l] (FP64 form): n.
   {
     const int a = tid >> 5, l = tid & 31;
     if (a < 3) {
@@ -231,7 +308,7 @@ __global__ void __launch_bounds__(256, FP64 ? 2 : 4) k_pair(const PairArgs A) {
         const int n = nimg(l);
         (a == 0 ? ox : (a == 1 ? oy : oz))[l] = fmaf((float)(2 * (l - 1) - t), 0.5f * blf, (float)n * rf);
         if (l < E) {
-          if (FP64) (a == 0 ? imx : (a == 1 ? imy : imz))[l] = n * B.L[a];
+          if (FP64) img[32 * a + l] = (signed char)n;
           if (a > 0) {
             float* dt = a == 1 ? dyt : dzt;
 #pragma unroll
@@ -327,211 +404,107 @@ __global__ void __launch_bounds__(256, FP64 ? 2 : 4) k_pair(const PairArgs A) {
   double esum = 0.0, wsum = 0.0;  // FP64 form
   FixSum ek, wk;                  // mixed form: exact fixed-point sums of FP32 terms
   int ncand = 0, neval = 0, nacc = 0;
-  // per-warp item buffer: int4 (i | r << 16, lo1, lo2, n1 | n2 << 16)
-  int4* items = (int4*)(smem + L.items) + warp * kItems;
-  // per-warp queue of accepted pairs (mixed form)
-  float4* qd = (float4*)(smem + L.queue) + warp * kItems;
-  int* qk = (int*)(smem + L.queue + 16 * kItems * nw) + warp * kItems;
+  // per-warp queue of accepted pairs
+  // (mixed: separation and r^2, plus the key; FP64 form: the key only)
+  constexpr int kQd = FP64 ? 0 : 16;
+  float4* qd = (float4*)(smem + L.queue) + warp * kQueue;
+  int* qk = (int*)(smem + L.queue + kQd * kQueue * nw) + warp * kQueue;
+  // per-warp table of one step's items: (C, key base)
+  float4* ptA = (float4*)(smem + L.queue + (kQd + 4) * kQueue * nw) + warp * 32;
   int qn = 0;
   const unsigned lt = (1u << lane) - 1u;
-  int nbuf = 0;
+  const unsigned le = FULL >> (31 - lane);
+  unsigned char* r2l = smem + L.r2l + 64 * warp;  // two rank -> lane tables of 32
 
-  // per-warp table of the items of one mixed-form pass: (C, key base) and
-  // (lo1, n1, lo2 - n1, first candidate index)
-  float4* ptA = (float4*)(smem + L.queue + 20 * kItems * nw) + warp * 32;
-  int4* ptB = items;
-
-  // ---- one pass over the first min(nbuf, 32) items ----
+  // ---- consume one step's items, at most one per lane (nt = 0: none) ----
   // Mixed form: the items' candidate pairs are laid end to end and the warp
   // walks them 32 at a time, one pair per lane, so no lane idles while another
   // finishes a long j-range.  A lane finds its item from the bitmask of the
-  // items that start in the current 32 candidates.  FP64 form: one item per
-  // lane, each lane walks its own j-ranges.
-  auto run_pass = [&]() {
-    if (FP64 && nbuf > 32) {
-      // Put the 32 longest items first (4 length buckets, stable), so that a
-      // pass holds items of similar length and the short ones wait for more.
-      const int4 a = items[lane];
-      const bool hb = lane + 32 < nbuf;
-      const int4 bb = hb ? items[lane + 32] : make_int4(0, 0, 0, 0);
-      const int na = (a.w & 0xffff) + (a.w >> 16), nb = hb ? (bb.w & 0xffff) + (bb.w >> 16) : -1;
-      const int ka = na >= 12 ? 0 : (na >= 7 ? 1 : (na >= 4 ? 2 : 3));
-      const int kb = !hb ? 4 : (nb >= 12 ? 0 : (nb >= 7 ? 1 : (nb >= 4 ? 2 : 3)));
-      int base = 0, pa = 0, pb = 0;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const unsigned ba = __ballot_sync(FULL, ka == k), bbk = __ballot_sync(FULL, kb == k);
-        if (ka == k) pa = base + __popc(ba & lt);
-        if (kb == k) pb = base + __popc(ba) + __popc(bbk & lt);
-        base += __popc(ba) + __popc(bbk);
-      }
-      __syncwarp();
-      items[pa] = a;
-      if (hb) items[pb] = bb;
-      __syncwarp();
-    }
-    const int cnt = min(nbuf, 32);
-    int i = -1, r = 0, lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
-    if (lane < cnt) {
-      const int4 it = items[lane];
-      i = it.x & 0xffff;
-      r = it.x >> 16;
-      lo1 = it.y;
-      lo2 = it.z;
-      n1 = it.w & 0xffff;
-      n2 = it.w >> 16;
-    }
+  // items that start in the current 32 candidates.  FP64 form: each lane walks
+  // its own item's j-ranges.
+  auto consume = [&](int i, int r, int lo1, int n1, int lo2, int n2) {
     const int nt = n1 + n2;
-    const float4 pi = pf[i >= 0 ? i : 0];
-    const int ci = code[i >= 0 ? i : 0];
-    const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
-    const int dy = srows[2 * r], dz = srows[2 * r + 1];
-    const int ti = __float_as_int(pi.w);
-    if (!FP64) {
-      // exclusive scan of the items' candidate counts
-      int incl = nt;
+    const unsigned hb = __ballot_sync(FULL, nt > 0);
+    if (hb == 0u) return;
+    // exclusive scan of the items' candidate counts
+    int incl = nt;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += y;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int s0 = incl - nt;
+    const int T = __shfl_sync(FULL, incl, 31);
+    const int p1 = lo1 | (n1 << 16), l2 = lo2 - n1;
+    if (nt > 0) {
+      // the atom's position moved into the j-cells' frame: d = x_j + C
+      // (mixed: y, z relative to the cell origin; FP64: tile frame)
+      const float4 pi = pf[i];
+      const int ci = code[i];
+      const int ly = (ci >> 5) & 31, lz = ci >> 10;
+      const int dy = srows[2 * r], dz = srows[2 * r + 1];
+      const float Cy = FP64 ? -pi.y : dyt[ly * kDT + dy + 2] - pi.y;
+      const float Cz = FP64 ? -pi.z : dzt[lz * kDT + dz + 2] - pi.z;
+      ptA[lane] = make_float4(-pi.x, Cy, Cz, __int_as_float(i | (__float_as_int(pi.w) << 28)));
+      r2l[32 + __popc(hb & lt)] = (unsigned char)lane;
+    }
+    __syncwarp();
+    // distance tests (FP64 form: the FP32 prefilter); accepted pairs go to the
+    // warp's queue and their forces are computed in full batches of 32
+    int qb = 0;  // items that start before K
+    for (int K = 0; K < T; K += 32) {
+      const unsigned M = __reduce_or_sync(FULL, (nt > 0 && (unsigned)(s0 - K) < 32u) ? 1u << (s0 - K) : 0u);
+      const int qr = qb + __popc(M & le) - 1;  // >= 0: the first item starts at 0
+      qb += __popc(M);
+      const int ql = r2l[32 + qr];
+      const int bp1 = __shfl_sync(FULL, p1, ql), bl2 = __shfl_sync(FULL, l2, ql), bs = __shfl_sync(FULL, s0, ql);
+      const float4 a = ptA[ql];
+      const int k = K + lane;
+      const bool valid = k < T;
+      const int mo = k - bs;
+      const int m = mo < (bp1 >> 16) ? (bp1 & 0xffff) + mo : bl2 + mo;
+      const float4 pj = pf[valid ? m : 0];
+      float4 dq;
+      dq.x = pj.x + a.x;
+      dq.y = pj.y + a.y;
+      dq.z = pj.z + a.z;
+      dq.w = fmaf(dq.x, dq.x, fmaf(dq.y, dq.y, dq.z * dq.z));
+      const int tj = __float_as_int(pj.w);
+      const int kb = __float_as_int(a.w);
+      if (COUNT && valid) ++neval;
+      const float thr = FP64 ? rcpre : (MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2);
+      const bool acc = valid && dq.w <= thr;
+      const unsigned bal = __ballot_sync(FULL, acc);
+      if (acc) {
+        const int p = qn + __popc(bal & lt);
+        if (!FP64) qd[p] = dq;
+        qk[p] = kb | (m << 14) | (tj << 30);
+        if (!FP64 && COUNT) ++nacc;
       }
-      const int s0 = incl - nt;
-      const int T = __shfl_sync(FULL, incl, 31);
-      __syncwarp();
-      if (lane < cnt) {
-        // the atom's position moved into the j-cells' frame: d = x_j + C
-        const float Cx = -pi.x;
-        const float Cy = dyt[ly * kDT + dy + 2] - pi.y;
-        const float Cz = dzt[lz * kDT + dz + 2] - pi.z;
-        ptA[lane] = make_float4(Cx, Cy, Cz, __int_as_float(i | (ti << 28)));
-        ptB[lane] = make_int4(lo1, n1, lo2 - n1, s0);
-      }
-      __syncwarp();
-      // distance tests; accepted pairs go to the warp's queue and their forces
-      // are computed in full batches of 32 (force_batch)
-      int qbase = 0;  // items that start before K
-      for (int K = 0; K < T; K += 32) {
-        const unsigned M =
-            __reduce_or_sync(FULL, (lane < cnt && (unsigned)(s0 - K) < 32u) ? 1u << (s0 - K) : 0u);
-        const int q = qbase + __popc(M & (FULL >> (31 - lane))) - 1;  // item 0 starts at 0, so q >= 0
-        qbase += __popc(M);
-        const int k = K + lane;
-        const bool valid = k < T;
-        const float4 a = ptA[q];
-        const int4 b = ptB[q];
-        const int mo = k - b.w;
-        const int m = mo < b.y ? b.x + mo : b.z + mo;
-        const float4 pj = pf[valid ? m : 0];
-        float4 dq;
-        dq.x = pj.x + a.x;
-        dq.y = pj.y + a.y;
-        dq.z = pj.z + a.z;
-        dq.w = fmaf(dq.x, dq.x, fmaf(dq.y, dq.y, dq.z * dq.z));
-        const int tj = __float_as_int(pj.w);
-        const int kb = __float_as_int(a.w);
-        if (COUNT && valid) ++neval;
-        const float rc2 = MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
-        const bool acc = valid && dq.w <= rc2;
-        const unsigned bal = __ballot_sync(FULL, acc);
-        if (acc) {
-          const int p = qn + __popc(bal & lt);
-          qd[p] = dq;
-          qk[p] = kb | (m << 14) | (tj << 30);
-          if (COUNT) ++nacc;
-        }
-        qn += __popc(bal);
-        if (qn >= 32) {
-          __syncwarp();
+      qn += __popc(bal);
+      if (qn >= 32) {
+        __syncwarp();
+        if (FP64)
+          force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, nacc);
+        else
           force_batch<MULTI, ENERGY>(32, qd, qk, fa, fr, cap, A.lj, ek, wk);
-          __syncwarp();
-          const int rem = qn - 32;
-          float4 kd = make_float4(0.f, 0.f, 0.f, 0.f);
-          int kk = 0;
-          if (lane < rem) {
-            kd = qd[32 + lane];
-            kk = qk[32 + lane];
-          }
-          __syncwarp();
-          if (lane < rem) {
-            qd[lane] = kd;
-            qk[lane] = kk;
-          }
-          qn = rem;
-          __syncwarp();
+        __syncwarp();
+        const int rem = qn - 32;
+        float4 kd = make_float4(0.f, 0.f, 0.f, 0.f);
+        int kk = 0;
+        if (lane < rem) {
+          if (!FP64) kd = qd[32 + lane];
+          kk = qk[32 + lane];
         }
-      }
-    } else {
-      // FP32 prefilter on tile-frame coordinates, then the reference's FP64
-      // arithmetic (SRC/exaMD_forces.f90:509-523, user_func.f90:52-69)
-      double xi = 0, yi = 0, zi = 0, sy = 0, sz = 0, sxi = 0;
-      if (i >= 0) {
-        xi = pd[i];
-        yi = pd[cap + i];
-        zi = pd[2 * cap + i];
-        const int lyj = min(max(ly + dy, 0), EY - 1), lzj = min(max(lz + dz, 0), EZ - 1);
-        sy = imy[lyj] - imy[ly];
-        sz = imz[lzj] - imz[lz];
-        sxi = imx[lx];
-      }
-      const int tmax = warp_max(nt);
-      double ax = 0, ay = 0, az = 0;
-      for (int t = 0; t < tmax; ++t) {
-        if (t < nt) {
-          const int m = t < n1 ? lo1 + t : lo2 + (t - n1);
-          const float4 q = pf[m];
-          if (COUNT) ++neval;
-          const float fxp = q.x - pi.x, fyp = q.y - pi.y, fzp = q.z - pi.z;
-          const float r2f = fmaf(fxp, fxp, fmaf(fyp, fyp, fzp * fzp));
-          if (r2f <= rcpre) {
-            const int lxj = code[m] & 31;
-            const double sx = imx[lxj] - sxi;
-            double dx = __dsub_rn(pd[m], xi);
-            double dyv = __dsub_rn(pd[cap + m], yi);
-            double dzv = __dsub_rn(pd[2 * cap + m], zi);
-            // periodic image: physical separation = (x_j - x_i) + (n_j - n_i) L,
-            // exact (Sterbenz), equal to the reference's dx - Nint(dx/L) L
-            if (sx != 0.0) dx = __dadd_rn(dx, sx);
-            if (sy != 0.0) dyv = __dadd_rn(dyv, sy);
-            if (sz != 0.0) dzv = __dadd_rn(dzv, sz);
-            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dyv, dyv)), __dmul_rn(dzv, dzv));
-            LJ64 P = q64;
-            if (MULTI) P = A.lj.p64[ti * A.lj.nt + __float_as_int(q.w)];
-            if (d2 <= P.rc2) {
-              const double d2i = __drcp_rn(d2);
-              const double tt = __dmul_rn(P.sig2, d2i);
-              const double d6 = __dmul_rn(__dmul_rn(tt, tt), tt);
-              const double d12 = __dmul_rn(d6, d6);
-              const double dg = -__dmul_rn(__dmul_rn(P.eps24, __dsub_rn(__dmul_rn(2.0, d12), d6)), d2i);
-              const double fx = __dmul_rn(dg, dx), fy = __dmul_rn(dg, dyv), fz = __dmul_rn(dg, dzv);
-              ax += fx;
-              ay += fy;
-              az += fz;
-              atomicAdd(&fd[m], -fx);
-              atomicAdd(&fd[cap + m], -fy);
-              atomicAdd(&fd[2 * cap + m], -fz);
-              if (ENERGY) {
-                esum += __dmul_rn(P.eps4, __dsub_rn(d12, d6));
-                wsum += -__dmul_rn(dg, d2);
-              }
-              if (COUNT) ++nacc;
-            }
-          }
+        __syncwarp();
+        if (lane < rem) {
+          if (!FP64) qd[lane] = kd;
+          qk[lane] = kk;
         }
-      }
-      if (nt > 0) {
-        atomicAdd(&fd[i], ax);
-        atomicAdd(&fd[cap + i], ay);
-        atomicAdd(&fd[2 * cap + i], az);
+        qn = rem;
+        __syncwarp();
       }
     }
-    // drop the processed items
-    __syncwarp();
-    const int rem = nbuf - cnt;
-    int4 keep = make_int4(0, 0, 0, 0);
-    if (lane < rem) keep = items[32 + lane];
-    __syncwarp();
-    if (lane < rem) items[lane] = keep;
-    nbuf = rem;
     __syncwarp();
   };
 
@@ -548,7 +521,6 @@ __global__ void __launch_bounds__(256, FP64 ? 2 : 4) k_pair(const PairArgs A) {
   const int nunits = 2 * ((total + 31) >> 5);
   const float prune2 = A.lj.prune2;
   int* ucnt = (int*)(red + 8 * nw);
-  unsigned char* r2l = smem + L.r2l + 32 * warp;  // rank among working lanes -> lane
   while (true) {
     int u = 0;
     if (lane == 0) u = atomicAdd(ucnt, 1);
@@ -643,18 +615,16 @@ __global__ void __launch_bounds__(256, FP64 ? 2 : 4) k_pair(const PairArgs A) {
           }
         }
       }
-      const unsigned b = __ballot_sync(FULL, n1 > 0);
-      if (n1 > 0) items[nbuf + __popc(b & lt)] = make_int4(i | (r << 16), lo1, lo2, n1 | (n2 << 16));
-      nbuf += __popc(b);
-      __syncwarp();
-      if (nbuf >= 32) run_pass();
+      consume(i, r, lo1, n1, lo2, n2);
     }
     __syncwarp();
   }
-  while (nbuf > 0) run_pass();
-  if (!FP64 && qn > 0) {  // the last, partial batch
+  if (qn > 0) {  // the last, partial batch
     __syncwarp();
-    force_batch<MULTI, ENERGY>(qn, qd, qk, fa, fr, cap, A.lj, ek, wk);
+    if (FP64)
+      force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, nacc);
+    else
+      force_batch<MULTI, ENERGY>(qn, qd, qk, fa, fr, cap, A.lj, ek, wk);
   }
   __syncthreads();
 
