@@ -99,7 +99,7 @@ bool build_own_lut(OwnLut& L) {
   return true;
 }
 
-int round_block_length(double want, double* out) {
+int round_block_length(double want, double* out, int* q_out, int* k_out) {
   if (!(want > 0.0) || !std::isfinite(want)) return EXAMD_ERR_ARG;
   // largest k with ceil(want * 2^k) < 2^14: c * bl then needs <= 24 bits
   int k = 13 - (int)std::floor(std::log2(want));
@@ -108,11 +108,13 @@ int round_block_length(double want, double* out) {
     double q = std::ceil(want * std::ldexp(1.0, k));
     if (q < 16384.0) {
       bl = std::ldexp(q, -k);
+      *q_out = (int)q;
+      *k_out = k;
       break;
     }
   }
   if (!(bl >= want)) return EXAMD_ERR_ARG;
-  *out = bl;
+  *out = bl;  // = q * 2^-k
   return EXAMD_OK;
 }
 
@@ -340,7 +342,8 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   double want = p.cell_edge > 0 ? p.cell_edge : 0.5 * rcmax;
   if (want < 0.5 * rcmax) return EXAMD_ERR_ARG;
   double bl;
-  if (round_block_length(want, &bl) != EXAMD_OK) return EXAMD_ERR_ARG;
+  int blq = 0, blk = 0;
+  if (round_block_length(want, &bl, &blq, &blk) != EXAMD_OK) return EXAMD_ERR_ARG;
 
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1 || p.device < 0 || p.device >= ndev)
@@ -434,6 +437,8 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     }
     B.bl = bl;
     B.bli = 1.0 / bl;
+    B.blq = blq;
+    B.blk = blk;
     for (int a = 0; a < 3; ++a) B.remf[a] = (float)(B.L[a] - B.nb[a] * bl);  // nb*bl is exact
     B.blf = (float)bl;
     B.blif = (float)(1.0 / bl);
@@ -816,6 +821,10 @@ KickArgs kick_args(examd_ctx* ctx, double ckick, double dt, bool drift, double h
   k.dt = dt;
   k.drift = drift;
   k.hk = hk;
+  for (int t = 0; t < EXAMD_MAX_TYPES; ++t) {
+    k.ckm[t] = ckick * ctx->lj.minv[t];
+    k.hkm[t] = hk * ctx->lj.minv[t];
+  }
   k.boxKE = boxKE;
   k.keAtom = ctx->keAtom;
   k.atom0 = ctx->d_atom0;

@@ -11,41 +11,19 @@
 
 namespace examd {
 
-// Cell of one coordinate and the offset from the cell origin c * bl.  bl has at
-// most 13 significant bits, so c * bl is exact in FP32 and x - c * bl is exact
-// in FP64: the cell is exactly Int(x / bl) of the exact quotient, with the
-// last cell absorbing the remainder (SRC/exaMD_module.f90:109-113).
-__device__ __forceinline__ int cell_of(double x, float blf, float blif, int nb, float& u) {
-  float xh = (float)x;
-  int c = (int)(xh * blif);
-  c = min(max(c, 0), nb - 1);
-  double ud = x - (double)((float)c * blf);
-  if (ud < 0.0) {  // FP32 estimate one too high
-    c = max(c - 1, 0);
-    ud = x - (double)((float)c * blf);
-  } else if (c < nb - 1 && (float)ud >= blf) {  // possibly one too low
-    if (ud >= (double)blf) {
-      c += 1;
-      ud = x - (double)((float)c * blf);
-    }
-  }
-  u = (float)ud;
-  return c;
-}
-
 __device__ __forceinline__ void bin_one(int s, double x, double y, double z, int meta,
                                         const BoxDev* __restrict__ boxes, int* __restrict__ cellOld,
                                         int* __restrict__ slot, float4* __restrict__ Uold,
                                         int* __restrict__ count, int* __restrict__ status) {
   const BoxDev& B = boxes[meta >> 8];
-  if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+  if (!(finite_bits(x) && finite_bits(y) && finite_bits(z))) {
     atomicOr(status, ST_NONFINITE);
     x = y = z = 0.0;
   }
   float ux, uy, uz;
-  int cx = cell_of(x, B.blf, B.blif, B.nb[0], ux);
-  int cy = cell_of(y, B.blf, B.blif, B.nb[1], uy);
-  int cz = cell_of(z, B.blf, B.blif, B.nb[2], uz);
+  int cx = cell_offset(x, B, 0, ux);
+  int cy = cell_offset(y, B, 1, uy);
+  int cz = cell_offset(z, B, 2, uz);
   int gc = B.cell0 + cx + B.nb[0] * (cy + B.nb[1] * cz);
   cellOld[s] = gc;
   Uold[s] = make_float4(ux, uy, uz, __int_as_float(meta & 0xff));
@@ -69,8 +47,8 @@ __global__ void k_load_bin(int64_t n, const double* __restrict__ aos, const doub
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     double x = aos[3 * s + a];
-    if (strict && !(x >= 0.0 && x < B.L[a])) atomicOr(status, ST_OUTSIDE);
-    p[a] = isfinite(x) ? wrap_coord(x, B.L[a], B.Li[a], B.Lf[a]) : x;
+    if (strict && !in_range_bits(x, B.L[a])) atomicOr(status, ST_OUTSIDE);
+    p[a] = finite_bits(x) ? wrap_coord(x, B.L[a], B.Li[a]) : x;
   }
   X0[s] = p[0];
   X1[s] = p[1];
@@ -103,8 +81,8 @@ __global__ void k_gather_pos_bin(int64_t n, const double* __restrict__ aos, cons
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     double x = aos[3 * i + a];
-    if (strict && !(x >= 0.0 && x < B.L[a])) atomicOr(status, ST_OUTSIDE);
-    p[a] = isfinite(x) ? wrap_coord(x, B.L[a], B.Li[a], B.Lf[a]) : x;
+    if (strict && !in_range_bits(x, B.L[a])) atomicOr(status, ST_OUTSIDE);
+    p[a] = finite_bits(x) ? wrap_coord(x, B.L[a], B.Li[a]) : x;
   }
   X0[s] = p[0];
   X1[s] = p[1];

@@ -37,6 +37,7 @@ enum StatusBits : int {
 struct BoxDev {
   double L[3], Li[3];
   double bl, bli;  // block_length (cell edge) and its inverse
+  int blq, blk;    // bl = blq * 2^-blk exactly (blq < 2^14)
   float blf, blif, Lf[3];
   float remf[3];   // L - nb*bl: the extra width of the last cell, FP32
   int nb[3];
@@ -116,15 +117,88 @@ struct KSum {
   }
 };
 
-// Periodic wrap of an FP64 coordinate into [0, L); the common in-range case
-// is decided in FP32 (FP64 instructions are scarce on this part).
-__device__ __forceinline__ double wrap_coord(double x, double L, double Li, float Lf) {
-  float xf = (float)x;
-  if (xf > 1e-3f && xf < Lf - 1e-3f) return x;
+// FP64 arithmetic and the FP32 <-> FP64 conversions both run on this part's
+// FP64 pipe, 1/64 of the FP32 rate.  The per-atom kernels therefore decide
+// range, finiteness and cell membership of an FP64 coordinate on its bits
+// with integer operations, and spend FP64 instructions only on the arithmetic
+// that needs them.
+
+// 0 <= x < L (either zero), for L > 0: non-negative doubles are ordered as
+// their bit patterns, and every negative one has the sign bit set.
+__device__ __forceinline__ bool in_range_bits(double x, double L) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return b < (unsigned long long)__double_as_longlong(L) || b == 0x8000000000000000ull;
+}
+
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+
+// A float within one FP32 ulp of x (mantissa truncated), for estimates only;
+// 0 for |x| < 2^-126.  x must be below 2^128 in magnitude.
+__device__ __forceinline__ float d2f_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e < 1023 - 126) return 0.f;
+  return __uint_as_float((unsigned)(b >> 32 & 0x80000000u) | ((unsigned)(e - 1023 + 127) << 23) |
+                         (unsigned)((b >> 29) & 0x7fffff));
+}
+
+// x rounded to the nearest float, ties to even, for 0 <= x < 2^128; values
+// below 2^-126 become 0 (no subnormals).  Same result as (float)x in the
+// normal range.
+__device__ __forceinline__ float d2f_rn_nonneg(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+  const int e = (int)(b >> 52);
+  if (e < 1023 - 126) return 0.f;
+  const unsigned mf = (unsigned)((b >> 29) & 0x7fffff);
+  const unsigned long long rest = b & 0x1fffffffull;  // the 29 dropped mantissa bits
+  unsigned bits = ((unsigned)(e - 1023 + 127) << 23) | mf;
+  if (rest > 0x10000000ull || (rest == 0x10000000ull && (mf & 1u))) ++bits;  // a carry rounds up the exponent
+  return __uint_as_float(bits);
+}
+
+// n * 2^-k exactly, for 0 < n < 2^31 (0 for n = 0).
+__device__ __forceinline__ double mul_pow2(unsigned n, int k) {
+  if (n == 0u) return 0.0;
+  const int p = 31 - __clz(n);
+  const unsigned long long mant = ((unsigned long long)n << (52 - p)) & 0xfffffffffffffull;
+  return __longlong_as_double((long long)(((unsigned long long)(p - k + 1023) << 52) | mant));
+}
+
+// Cell c = Int(x / bl) of the exact quotient, clamped to the last cell (which
+// absorbs the remainder, SRC/exaMD_module.f90:109-113), and the offset
+// u = x - c*bl rounded once to FP32, for 0 <= x < L.  One FP64 subtraction:
+// the FP32 estimate of c is within one of the exact cell, c*bl and (c+1)*bl
+// are built exactly from their integer multiples of 2^-k and compared with x
+// as bit patterns, and x - c*bl is then exact.
+__device__ __forceinline__ int cell_offset(double x, const BoxDev& B, int a, float& u) {
+  const int nb = B.nb[a];
+  int c = (int)(d2f_trunc(x) * B.blif);
+  c = min(max(c, 0), nb - 1);
+  long long bx = __double_as_longlong(x);
+  if (bx == (long long)0x8000000000000000ull) bx = 0;  // -0
+  if (bx < __double_as_longlong(mul_pow2((unsigned)(c * B.blq), B.blk))) {
+    c = max(c - 1, 0);  // the estimate was one too high
+  } else if (c < nb - 1 && bx >= __double_as_longlong(mul_pow2((unsigned)((c + 1) * B.blq), B.blk))) {
+    ++c;  // one too low
+  }
+  u = d2f_rn_nonneg(x - mul_pow2((unsigned)(c * B.blq), B.blk));
+  return c;
+}
+
+// Periodic wrap of an FP64 coordinate into [0, L).  The in-range case is
+// decided on the bits; the rare out-of-range case is a separate function so
+// that its FP64 instructions are not executed speculatively by every thread.
+static __device__ __noinline__ double wrap_slow(double x, double L, double Li) {
   double y = x - floor(x * Li) * L;
   if (y >= L) y -= L;
   if (y < 0.0) y += L;
   return y;
+}
+
+__device__ __forceinline__ double wrap_coord(double x, double L, double Li) {
+  return in_range_bits(x, L) ? x : wrap_slow(x, L, Li);
 }
 
 }  // namespace examd

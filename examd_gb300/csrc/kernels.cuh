@@ -88,6 +88,8 @@ struct KickArgs {
   double dt;
   bool drift;
   double hk;        // > 0: also the kinetic energy at v + hk F / m, per box
+  double ckm[4];    // ckick / m per type
+  double hkm[4];    // hk / m per type
   double* keAtom;   // per-atom kinetic energy scratch (N)
   double* boxKE;    // per-box kinetic energy (fixed-order reduction of keAtom)
   const int64_t* atom0;  // nboxes + 1 atom offsets (sorted order is grouped by box)

@@ -1,9 +1,9 @@
 // Issue-rate probe of the pipes the pair kernel uses, on the GPU it runs on:
 // FP32 FMA (the pair kernel's roofline denominator), FP64 FMA (the FP64
-// form's), and the shared-memory atomics of the force sums (int32, fp32,
-// fp64).  Each kernel runs a fixed, bounded number of independent operations
-// per thread; every shared-memory index is masked into its array.  Prints one
-// JSON object.
+// form's), FP32 <-> FP64 conversions (the integrator's), and the shared-memory
+// atomics of the force sums (int32, fp32, fp64).  Each kernel runs a fixed,
+// bounded number of independent operations per thread; every shared-memory
+// index is masked into its array.  Prints one JSON object.
 //
 //   nvcc -O3 -gencode arch=compute_103a,code=sm_103a pipe_rates.cu -o pipe_rates
 #include <cuda_runtime.h>
@@ -45,6 +45,33 @@ __global__ void k_dfma(double* out, int iters) {
 #pragma unroll
       for (int k = 0; k < 4; ++k) a[k] = fma(a[k], 0.999, 1e-4);
   out[blockIdx.x * blockDim.x + threadIdx.x] = a[0] + a[1] + a[2] + a[3];
+}
+
+// FP64 -> FP32 and FP32 -> FP64 conversions: 4 independent chains per thread;
+// each step feeds the converted bits back through integer adds so that no
+// conversion can be folded away.
+__global__ void k_d2f(float* out, int iters) {
+  long long b[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) b[k] = __double_as_longlong(1.0 + 1e-3 * (threadIdx.x + k));
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) b[k] += __float_as_int((float)__longlong_as_double(b[k])) & 0xff;
+  out[blockIdx.x * blockDim.x + threadIdx.x] = (float)((b[0] ^ b[1] ^ b[2] ^ b[3]) & 0xffff);
+}
+
+__global__ void k_f2d(float* out, int iters) {
+  int b[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) b[k] = __float_as_int(1.f + 1e-3f * (threadIdx.x + k));
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) b[k] += __double2loint((double)__int_as_float(b[k])) & 0xff;
+  out[blockIdx.x * blockDim.x + threadIdx.x] = (float)((b[0] ^ b[1] ^ b[2] ^ b[3]) & 0xffff);
 }
 
 // Shared-memory atomic adds, 8 per iteration per thread, lanes on distinct
@@ -95,6 +122,8 @@ int main() {
   const int it = 2000;
   const double t_ffma = time_ms([&] { k_ffma<<<blocks, threads>>>(of, it); });
   const double t_dfma = time_ms([&] { k_dfma<<<blocks, threads>>>(od, it / 16); });
+  const double t_d2f = time_ms([&] { k_d2f<<<blocks, threads>>>(of, it / 16); });
+  const double t_f2d = time_ms([&] { k_f2d<<<blocks, threads>>>(of, it / 16); });
   const double t_ai = time_ms([&] { k_satom<int><<<blocks, threads>>>(of, it / 8); });
   const double t_af = time_ms([&] { k_satom<float><<<blocks, threads>>>(of, it / 8); });
   const double t_ad = time_ms([&] { k_satom<double><<<blocks, threads>>>(of, it / 64); });
@@ -107,9 +136,11 @@ int main() {
       "{\"device\": \"%s\", \"sms\": %d, \"clock_mhz\": %.0f, "
       "\"ffma_per_clk_sm\": %.2f, \"fp32_tflops\": %.2f, "
       "\"dfma_per_clk_sm\": %.3f, \"fp64_tflops\": %.3f, "
+      "\"cvt_f64_to_f32_per_clk_sm\": %.3f, \"cvt_f32_to_f64_per_clk_sm\": %.3f, "
       "\"smem_atomic_add_per_clk_sm\": {\"i32\": %.2f, \"f32\": %.2f, \"f64\": %.3f}}\n",
       pr.name, sms, hz * 1e-6, per_clk(ffma_ops, t_ffma), 2.0 * ffma_ops / (t_ffma * 1e-3) * 1e-12,
       per_clk(dfma_ops, t_dfma), 2.0 * dfma_ops / (t_dfma * 1e-3) * 1e-12,
+      per_clk((double)n * (it / 16) * 32, t_d2f), per_clk((double)n * (it / 16) * 32, t_f2d),
       per_clk((double)n * (it / 8) * 8, t_ai), per_clk((double)n * (it / 8) * 8, t_af),
       per_clk((double)n * (it / 64) * 8, t_ad));
   cudaFree(of);

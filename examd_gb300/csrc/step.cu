@@ -16,27 +16,10 @@ __device__ __forceinline__ void bin_store(int s, double x, double y, double z, i
                                           int* __restrict__ cellOld, int* __restrict__ slot,
                                           float4* __restrict__ Uold, int* __restrict__ count) {
   // same rule as bin.cu: exact cell of the FP64 position on the grid c * bl
-  auto cell_of = [](double x, float blf, float blif, int nb, float& u) {
-    float xh = (float)x;
-    int c = (int)(xh * blif);
-    c = min(max(c, 0), nb - 1);
-    double ud = x - (double)((float)c * blf);
-    if (ud < 0.0) {
-      c = max(c - 1, 0);
-      ud = x - (double)((float)c * blf);
-    } else if (c < nb - 1 && (float)ud >= blf) {
-      if (ud >= (double)blf) {
-        c += 1;
-        ud = x - (double)((float)c * blf);
-      }
-    }
-    u = (float)ud;
-    return c;
-  };
   float ux, uy, uz;
-  int cx = cell_of(x, B.blf, B.blif, B.nb[0], ux);
-  int cy = cell_of(y, B.blf, B.blif, B.nb[1], uy);
-  int cz = cell_of(z, B.blf, B.blif, B.nb[2], uz);
+  int cx = cell_offset(x, B, 0, ux);
+  int cy = cell_offset(y, B, 1, uy);
+  int cz = cell_offset(z, B, 2, uz);
   int gc = B.cell0 + cx + B.nb[0] * (cy + B.nb[1] * cz);
   cellOld[s] = gc;
   Uold[s] = make_float4(ux, uy, uz, __int_as_float(meta & 0xff));
@@ -178,13 +161,12 @@ __global__ void k_kick(const KickArgs k) {
   gather_force(k.s, ss, f);
   const int mt = k.meta[ss];
   const int type = mt & 0xff, box = mt >> 8;
-  const double minv = k.lj.minv[type];
-  const double ck = k.ckick * minv;
+  const double ck = k.ckm[type];
   double v[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) v[a] = k.V[a][ss];
   if (k.hk > 0.0) {
-    const double hm = k.hk * minv;
+    const double hm = k.hkm[type];
     double ke = 0.0;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -205,10 +187,10 @@ __global__ void k_kick(const KickArgs k) {
     double x[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      x[a] = wrap_coord(k.X[a][s] + k.dt * v[a], B.L[a], B.Li[a], B.Lf[a]);
+      x[a] = wrap_coord(fma(k.dt, v[a], k.X[a][s]), B.L[a], B.Li[a]);
       k.X[a][s] = x[a];
     }
-    if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) {
+    if (!(finite_bits(x[0]) && finite_bits(x[1]) && finite_bits(x[2]))) {
       atomicOr(k.status, ST_NONFINITE);
       x[0] = x[1] = x[2] = 0.0;
     }

@@ -20,8 +20,9 @@ box and the LJ parameters of the case:
 
     python -m examd_gb300.workloads --case liquid --nc 64 --precision mixed --evals 3
 
-runs `evals` force evaluations of one case on the GPU (a short, fixed launch
-sequence for profilers) and prints the pair counters and the device time.
+runs `evals` force evaluations of one case on the GPU, then `--steps`
+velocity-Verlet steps (a short, fixed launch sequence for profilers), and
+prints the pair counters.
 """
 from __future__ import annotations
 
@@ -122,6 +123,7 @@ def main(argv=None):
     ap.add_argument("--nboxes", type=int, default=512, help="ensemble: boxes")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--evals", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=0, help="then this many velocity-Verlet steps (dt 0.005)")
     ap.add_argument("--tile", type=int, default=None)
     a = ap.parse_args(argv)
     kw = {"liquid": {"nc": a.nc}, "slab": {"n": a.n}, "ensemble": {"nboxes": a.nboxes},
@@ -131,6 +133,8 @@ def main(argv=None):
         for _ in range(a.evals):
             s.forces()
         cnt = s.counters()
+        if a.steps:
+            s.run(a.steps, 0.005)
     print(json.dumps({"case": a.case, "atoms": int(case["natoms"].sum()), "boxes": len(case["natoms"]),
                       "precision": a.precision, "evals": a.evals, **cnt}))
 
