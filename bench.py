@@ -1,21 +1,28 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 midpoint Lennard-Jones path (one JSON line on stdout).
 
-Workload: 1,048,576 atoms (FCC 64^3 x 4) at rho* = 0.8442, melted at T* = 1.0,
-LJ eps = sigma = m = 1, rc = 2.5 sigma truncated and unshifted, dt = 0.005,
-velocity-Verlet with re-binning every step.  A step = one velocity-Verlet step
-over all atoms (kick + drift + wrap + binning + midpoint pair forces).
-Synthetic, seeded inputs; no dataset is involved.
+Default workload: 1,048,576 atoms (FCC 64^3 x 4) at rho* = 0.8442, melted at
+T* = 1.0, LJ eps = sigma = m = 1, rc = 2.5 sigma truncated and unshifted,
+dt = 0.005, velocity-Verlet with re-binning every step.  A step = one
+velocity-Verlet step over all atoms (kick + drift + wrap + binning + midpoint
+pair forces).  Synthetic, seeded inputs; no dataset is involved.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl examd|reference]
+                    [--workload liquid|liquid-rc3|slab|ensemble|mixture|fcc32k]
 
 value: atom-steps/s of the mixed form with all state resident in HBM, device
 time (CUDA events on the library's stream), max over ranks.  e2e: the same
 metric through the drop-in force call with host buffers (pinned positions in,
-forces out, every step).  --impl reference times the CPU restatement of the
+forces out, every step).  The line also carries the FP64 form's rate on the
+same atoms, the mixed form's force error against it and both forms' energy
+drift per 1000 steps.  --impl reference times the CPU restatement of the
 reference's force routine (oracle/) with all host threads on the same
 workload.  With N > 1 (torchrun) each rank runs an independent replica on its
 own GPU (the path has no inter-GPU exchange): scaling "weak".
+
+Other workloads (--workload) are the remaining configurations of the same
+metric: rc = 3.0; an uneven liquid slab in vapour; a batched ensemble of 512
+boxes; a 16.8M-atom binary mixture; the 32,000-atom FCC fluid at T* = 0.72.
 """
 from __future__ import annotations
 
@@ -33,9 +40,18 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 NC, RHO, RC, DT, T_MELT = 64, 0.8442, 2.5, 0.005, 1.0
-WORKLOAD = "lj-liquid-fcc64-1048576-rc2.5"
 METRIC = "atom-steps/s on 1 GB300: mixed-FP32 vs FP64 path at <=1e-5 RMS force rel. error"
 FP32_PEAK_TFLOPS = 73.84  # FFMA probe (python -m examd_gb300.peaks) on a GB300; used if the live probe fails
+
+# name -> (workload label, dt, equilibration steps, rescale interval, drift steps)
+WORKLOADS = {
+    "liquid": ("lj-liquid-fcc64-1048576-rc2.5", 0.005, 300, 50, 1000),
+    "liquid-rc3": ("lj-liquid-fcc64-1048576-rc3.0", 0.005, 300, 50, 1000),
+    "slab": ("lj-slab-524288-rho0.75-in-vapour0.02-Lz4Lx-rc3.0", 0.005, 200, 20, 500),
+    "ensemble": ("lj-ensemble-512-boxes-256-16384-rc2.5", 0.005, 200, 20, 1000),
+    "mixture": ("lj-binary-mixture-16777216-80-20-rho1.2-rc2.5sigma", 0.003, 200, 20, 1000),
+    "fcc32k": ("lj-fcc-32000-rho0.8442-T0.72-rc2.5", 0.005, 0, 0, 1000),
+}
 
 
 def dist_info():
@@ -73,13 +89,38 @@ def build_liquid(ex, seed=1):
     return pos, vel, L
 
 
-def melt(sysm, n, steps=300, every=50):
-    """Melt the lattice: hot start, velocity rescaling to T_MELT every `every` steps."""
-    for _ in range(steps // every):
-        sysm.run(every, DT)
-        ek = sysm.kinetic()[0]
-        T = 2.0 * ek / (3.0 * (n - 1))
-        sysm.scale_velocities(np.sqrt(T_MELT / T))
+def make_case(name, seed):
+    """Atoms, boxes and LJ parameters of a workload, plus each box's target temperature."""
+    import examd_gb300 as ex
+    from examd_gb300 import workloads as W
+    if name in ("liquid", "liquid-rc3"):
+        pos, vel, L = build_liquid(ex, seed)  # hot start at 2 T*, melted by the equilibration
+        case = {"pos": pos, "vel": vel, "types": None, "boxes": np.full((1, 3), L), "natoms": np.array([len(pos)]),
+                "lj": {"rc": 3.0 if name == "liquid-rc3" else RC}}
+        return case, np.array([T_MELT])
+    if name == "slab":
+        return W.slab(seed=seed + 2), np.array([0.85])
+    if name == "ensemble":
+        c = W.ensemble(seed=seed + 3)
+        return c, c["temperatures"]
+    if name == "mixture":
+        return W.binary_mixture(seed=seed + 4), np.array([1.0])
+    if name == "fcc32k":
+        pos, L = ex.gen_fcc(20, RHO)
+        vel = ex.gen_velocities(len(pos), 0.72, seed)
+        case = {"pos": pos, "vel": vel, "types": None, "boxes": np.full((1, 3), L), "natoms": np.array([len(pos)]),
+                "lj": {"rc": RC}}
+        return case, np.array([0.72])
+    raise ValueError(name)
+
+
+def equilibrate(sysm, natoms, temps, steps, every, dt):
+    """steps velocity-Verlet steps, rescaling each box to its target temperature every `every` steps."""
+    dof = 3.0 * np.maximum(np.asarray(natoms, dtype=np.float64) - 1.0, 1.0)
+    for _ in range(steps // every if every else 0):
+        sysm.run(every, dt)
+        T = 2.0 * sysm.kinetic() / dof
+        sysm.scale_velocities(np.sqrt(temps / np.maximum(T, 1e-12)))
 
 
 class ClockSampler:
@@ -156,11 +197,11 @@ def fp32_peak():
         return FP32_PEAK_TFLOPS, f"of measured earlier (profiles/gb300_pipe_rates.txt); live probe failed: {e}"
 
 
-def drift_per_1000(e):
-    """Least-squares slope of (E - E0)/|E0| per 1000 steps."""
+def drift_per_1000(e, scale=None):
+    """Least-squares slope of (E - E0)/|E0| per 1000 steps (or of (E - E0)/scale)."""
     e = np.asarray(e, dtype=np.float64)
     s = np.arange(len(e))
-    y = (e - e[0]) / abs(e[0])
+    y = (e - e[0]) / (abs(e[0]) if scale is None else scale)
     return float(np.polyfit(s, y, 1)[0] * 1000.0)
 
 
@@ -183,6 +224,10 @@ def run_reference(args, ws, rk):
     """CPU restatement of the reference path, all host threads, same workload."""
     if rk != 0:
         return
+    if args.workload != "liquid":
+        print(json.dumps({"impl": "reference", "unavailable": f"the CPU arm covers the default workload only, "
+                                                              f"not {args.workload}"}), flush=True)
+        return
     import examd_gb300 as ex
     from oracle import oracle as O
     O.build()
@@ -199,8 +244,8 @@ def run_reference(args, ws, rk):
     line = {"metric": METRIC, "value": v, "unit": "atom-steps/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "atoms": len(pos), "rc": RC, "dt": DT, "precision": "fp64",
-                       "l2": "working set > L2"},
+            "config": {"workload": WORKLOADS["liquid"][0], "atoms": len(pos), "rc": RC, "dt": DT,
+                       "precision": "fp64", "l2": "working set > L2"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": cores, "kind": "port",
                              "sample": f"{args.steps} velocity-Verlet steps (force evaluation by the C restatement "
@@ -217,7 +262,9 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="examd", choices=["examd", "reference"])
+    ap.add_argument("--workload", default="liquid", choices=sorted(WORKLOADS))
     ap.add_argument("--chunk", type=int, default=20, help="steps per captured CUDA graph")
+    ap.add_argument("--drift-steps", type=int, default=None, help="steps of the energy-drift runs")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 / drift side measurements")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
@@ -232,20 +279,24 @@ def main():
     import examd_gb300 as ex
     from examd_gb300 import build as B
     B.build()
-    pos, vel, L = build_liquid(ex, seed=1 + rk)
-    n = len(pos)
-    box = np.full(3, L)
-    sysm = ex.MidpointLJ(box, [n], precision="mixed", rc=RC, device=lr)
-    sysm.set_atoms(pos, vel=vel)
-    melt(sysm, n)
+    label, dt, eq_steps, eq_every, drift_steps = WORKLOADS[args.workload]
+    if args.drift_steps is not None:
+        drift_steps = args.drift_steps
+    case, temps = make_case(args.workload, 1 + rk)
+    n = int(case["natoms"].sum())
+    nboxes = len(case["natoms"])
+    lj = dict(case["lj"])
+    sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **lj)
+    sysm.set_atoms(case["pos"], case["types"], case["vel"])
+    equilibrate(sysm, case["natoms"], temps, eq_steps, eq_every, dt)
     chunk = max(2, args.chunk // 2 * 2)
     wsteps = max(args.warmup, chunk + 2)
     wsteps += wsteps % 2
-    sysm.run(wsteps, DT, graph_chunk=chunk)  # warm-up; captures the graph (even count keeps buffer parity)
+    sysm.run(wsteps, dt, graph_chunk=chunk)  # warm-up; captures the graph (even count keeps buffer parity)
 
     barrier(dist)
     with ClockSampler(lr) as clk:
-        out = sysm.run(args.steps, DT, graph_chunk=chunk)
+        out = sysm.run(args.steps, dt, graph_chunk=chunk)
     barrier(dist)
     t_ms = allmax(dist, out["ms"])
     value = n * args.steps * ws / (t_ms * 1e-3)
@@ -257,12 +308,12 @@ def main():
     reps = 20
     _, k_ms = sysm.time_forces(reps)
     achieved = flops / (k_ms * 1e-3) / 1e12
-    traffic = read_traffic()
+    traffic = read_traffic() if args.workload == "liquid" else None
 
     # end to end through the drop-in force call with pinned host buffers
-    melted, _ = sysm.state()
+    state, _ = sysm.state()
     hp = ex.pinned_empty((n, 3))
-    hp[:] = melted
+    hp[:] = state
     hf = ex.pinned_empty((n, 3))
     sysm.forces_at(hp, out=hf)
     e2e_steps = max(args.steps // 2, 10)
@@ -276,32 +327,50 @@ def main():
     extra = {}
     if not args.no_accuracy:
         f32, e32, _ = sysm.forces(energy=True)
-        _, vmel = sysm.state()
-        with ex.MidpointLJ(box, [n], precision="fp64", rc=RC, device=lr) as s64:
-            s64.set_atoms(melted, vel=vmel)
+        pos_now, vel_now = sysm.state()
+        with ex.MidpointLJ(case["boxes"], case["natoms"], precision="fp64", device=lr, **lj) as s64:
+            s64.set_atoms(pos_now, case["types"], vel_now)
             f64, e64, _ = s64.forces(energy=True)
             err = np.sqrt(((f32 - f64) ** 2).sum(1))
             fr = np.sqrt((f64 * f64).sum(1).mean())
-            s64.run(4, DT)
+            s64.run(4, dt)
             k64 = 10
-            o64 = s64.run(k64, DT)
+            o64 = s64.run(k64, dt)
             v64 = n * k64 / (o64["ms"] * 1e-3)
-            d64 = s64.run(1000, DT, graph_chunk=50, energies=True)
-        dm = sysm.run(1000, DT, graph_chunk=50, energies=True)
+            d64 = s64.run(drift_steps, dt, graph_chunk=50, energies=True)
+        dm = sysm.run(drift_steps, dt, graph_chunk=50, energies=True)
+        em = dm["ekin"] + dm["epot"]
+        e6 = d64["ekin"] + d64["epot"]
+        drift_m = [drift_per_1000(em[:, b]) for b in range(nboxes)]
+        drift_d = [drift_per_1000(e6[:, b]) for b in range(nboxes)]
         extra = {"fp64": {"value": v64, "ms_per_step": o64["ms"] / k64},
                  "mixed_over_fp64": value / ws / v64,
                  "force_rel_err_vs_fp64": {"rms": float(np.sqrt((err * err).mean()) / fr),
                                            "max": float(err.max() / fr)},
-                 "epot_rel_err_vs_fp64": float(abs(e32[0] - e64[0]) / abs(e64[0])),
-                 "energy_drift_per_1000_steps": {
-                     "mixed": drift_per_1000(dm["ekin"][:, 0] + dm["epot"][:, 0]),
-                     "fp64": drift_per_1000(d64["ekin"][:, 0] + d64["epot"][:, 0])}}
+                 "epot_rel_err_vs_fp64": float(np.abs(e32.sum() - e64.sum()) / abs(e64.sum())),
+                 "energy_drift_per_1000_steps": {"mixed": drift_m[0], "fp64": drift_d[0], "steps": drift_steps}}
+        if nboxes > 1:
+            # a box's total energy can be near zero (gas-like boxes), which makes
+            # (E - E0)/|E0| meaningless there: also report (E - E0)/<Ekin>
+            km, k6 = dm["ekin"].mean(0), d64["ekin"].mean(0)
+            am, ad = np.abs(drift_m), np.abs(drift_d)
+            bm = np.abs([drift_per_1000(em[:, b], km[b]) for b in range(nboxes)])
+            bd = np.abs([drift_per_1000(e6[:, b], k6[b]) for b in range(nboxes)])
+            extra["energy_drift_per_1000_steps"] = {
+                "mixed": {"median_abs": float(np.median(am)), "max_abs": float(am.max()),
+                          "median_abs_vs_ekin": float(np.median(bm)), "max_abs_vs_ekin": float(bm.max())},
+                "fp64": {"median_abs": float(np.median(ad)), "max_abs": float(ad.max()),
+                         "median_abs_vs_ekin": float(np.median(bd)), "max_abs_vs_ekin": float(bd.max())},
+                "per_box": "per-box drift; median and max of |drift| over the boxes, relative to |E0| and "
+                           "to the box's mean kinetic energy", "steps": drift_steps}
 
     line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": wsteps, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "atoms": n, "rc": RC, "dt": DT, "precision": "mixed",
-                       "graph_chunk": chunk, "l2": "working set > L2 (per-step HBM traffic ~0.2 GB)",
+            "config": {"workload": label, "atoms": n, "boxes": nboxes, "rc": lj.get("rc"), "dt": dt,
+                       "precision": "mixed", "graph_chunk": chunk,
+                       "l2": "working set > L2 (per-step HBM traffic ~0.2 KB per atom)" if n * 200 > 129e6
+                       else "working set fits L2 (small configuration)",
                        "parallelism": f"replicas{ws}"},
             "clocks": clk.summary(),
             "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n},
@@ -312,8 +381,8 @@ def main():
                          "candidates": cnt["candidates"], "accepted": cnt["accepted"],
                          "peak_source": peak_src},
             **extra}
-    if rk == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(melted, L)
+    if rk == 0 and not args.no_cpu and args.workload == "liquid":
+        line["cpu_baseline"] = cpu_baseline(state, case["boxes"][0, 0])
     if rk == 0:
         print(json.dumps(line), flush=True)
     sysm.close()

@@ -174,6 +174,8 @@ struct examd_ctx {
   double* d_factor = nullptr;
   int64_t* d_atom0 = nullptr;
   double* keAtom = nullptr;
+  double* partial = nullptr;  // chunk partial sums of the per-box reductions
+  int maxc_atoms = 1, maxc_tiles = 1;
   int ebuf_steps = 0;
 
   bool atoms_set = false;
@@ -218,7 +220,7 @@ void free_all(examd_ctx* ctx) {
                   ctx->cellOld, ctx->slot, ctx->src, ctx->count, ctx->cstart, ctx->bsum, ctx->d_total,
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
                   ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor,
-                  ctx->d_atom0, ctx->keAtom};
+                  ctx->d_atom0, ctx->keAtom, ctx->partial};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (int b = 0; b < 2; ++b) {
@@ -568,6 +570,16 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   ALLOC(ctx->d_factor, nboxes);
   ALLOC(ctx->d_atom0, nboxes + 1);
   ALLOC(ctx->keAtom, N);
+  {
+    int64_t maxa = 1, maxt = 1;
+    for (int b = 0; b < nboxes; ++b) {
+      maxa = std::max<int64_t>(maxa, ctx->atom0[b + 1] - ctx->atom0[b]);
+      maxt = std::max<int64_t>(maxt, ctx->tile0[b + 1] - ctx->tile0[b]);
+    }
+    ctx->maxc_atoms = red_chunks(maxa);
+    ctx->maxc_tiles = red_chunks(maxt);
+    ALLOC(ctx->partial, std::max((size_t)nboxes * ctx->maxc_atoms, (size_t)2 * nboxes * ctx->maxc_tiles));
+  }
 #undef ALLOC
   cudaStream_t st = ctx->st;
   bool ok = cudaMemcpyAsync(ctx->d_boxes, ctx->bh.data(), nboxes * sizeof(BoxDev), cudaMemcpyHostToDevice, st) ==
@@ -700,7 +712,8 @@ int run_pair(examd_ctx* ctx, bool energy, bool count, double* boxE = nullptr, do
   c.count = count;
   CK(launch_pair(c, pair_args(ctx), ctx->ntiles, ctx->smem, ctx->st));
   if (energy)
-    CK(launch_reduce_tiles(ctx->nboxes, ctx->d_tile0, ctx->tileE, ctx->tileW, boxE ? boxE : ctx->boxE,
+    CK(launch_reduce_tiles(ctx->nboxes, ctx->d_tile0, ctx->maxc_tiles, ctx->tileE, ctx->tileW, ctx->partial,
+                           boxE ? boxE : ctx->boxE,
                            boxW ? boxW : ctx->boxW, ctx->st));
   return EXAMD_OK;
 }
@@ -827,6 +840,8 @@ KickArgs kick_args(examd_ctx* ctx, double ckick, double dt, bool drift, double h
   }
   k.boxKE = boxKE;
   k.keAtom = ctx->keAtom;
+  k.partial = ctx->partial;
+  k.maxc = ctx->maxc_atoms;
   k.atom0 = ctx->d_atom0;
   k.nboxes = ctx->nboxes;
   k.lj = ctx->lj;
@@ -1012,7 +1027,8 @@ int examd_gpu_kinetic(examd_ctx* ctx, double* ekin) {
   if (!ctx->atoms_set) return EXAMD_ERR_STATE;
   cudaSetDevice(ctx->dev);
   const int c = ctx->cur;
-  CK(launch_kinetic(ctx->N, ctx->nboxes, ctx->d_atom0, ctx->V[c], ctx->meta[c], ctx->lj, ctx->keAtom, ctx->boxKE,
+  CK(launch_kinetic(ctx->N, ctx->nboxes, ctx->d_atom0, ctx->maxc_atoms, ctx->V[c], ctx->meta[c], ctx->lj,
+                    ctx->keAtom, ctx->partial, ctx->boxKE,
                     ctx->st));
   CK(cudaMemcpyAsync(ekin, ctx->boxKE, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));

@@ -76,8 +76,13 @@ struct StepArgs {
 // F = Fown + halo partials, in caller order, AoS doubles (out[3*id + a]); += if accumulate.
 cudaError_t launch_forces_out(const StepArgs& s, const int* id, double* out, int accumulate, cudaStream_t st);
 // Per-box sums of the per-tile energy/virial partials (FP64, fixed order).
-cudaError_t launch_reduce_tiles(int nboxes, const int* tile0, const double* tileE, const double* tileW,
-                                double* boxE, double* boxW, cudaStream_t st);
+// Per-box sums in two fixed-order levels (chunks of 4096 entries, then the
+// box's chunks in order); partial holds nboxes * maxc doubles (tiles: twice).
+int red_chunks(int64_t max_per_box);
+cudaError_t launch_reduce_tiles(int nboxes, const int* tile0, int maxc, const double* tileE, const double* tileW,
+                                double* partial, double* boxE, double* boxW, cudaStream_t st);
+cudaError_t launch_box_sums(int nboxes, const int64_t* atom0, int maxc, const double* v, double* partial,
+                            double* out, cudaStream_t st);
 // Velocity-Verlet pieces.  kick: v += c_kick F / m.  With drift: x += dt v, wrap, bin.
 struct KickArgs {
   StepArgs s;
@@ -92,6 +97,8 @@ struct KickArgs {
   double hkm[4];    // hk / m per type
   double* keAtom;   // per-atom kinetic energy scratch (N)
   double* boxKE;    // per-box kinetic energy (fixed-order reduction of keAtom)
+  double* partial;  // chunk partial sums of that reduction
+  int maxc;         // chunks per box
   const int64_t* atom0;  // nboxes + 1 atom offsets (sorted order is grouped by box)
   int nboxes;
   LJTable lj;
@@ -103,8 +110,9 @@ struct KickArgs {
   int* status;
 };
 cudaError_t launch_kick(const KickArgs& k, cudaStream_t st);
-cudaError_t launch_kinetic(int64_t n, int nboxes, const int64_t* atom0, const double* const V[3], const int* meta,
-                           LJTable lj, double* keAtom, double* boxKE, cudaStream_t st);
+cudaError_t launch_kinetic(int64_t n, int nboxes, const int64_t* atom0, int maxc, const double* const V[3],
+                           const int* meta, LJTable lj, double* keAtom, double* partial, double* boxKE,
+                           cudaStream_t st);
 cudaError_t launch_reduce_atoms(int nboxes, const int64_t* atom0, const double* v, double* out, cudaStream_t st);
 cudaError_t launch_scale_v(int64_t n, double* V[3], const int* meta, const double* factor, cudaStream_t st);
 cudaError_t launch_state_out(int64_t n, const double* const A[3], const int* id, double* out, cudaStream_t st);

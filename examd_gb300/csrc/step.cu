@@ -7,6 +7,8 @@
 // forces into the owner's blocks (SRC/exaMD_comms.f90:330-376).  All of these
 // are HBM-bound; FP64 is used only where positions, velocities and the
 // reductions need it.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -95,35 +97,80 @@ cudaError_t launch_forces_out(const StepArgs& s, const int* id, double* out, int
 }
 
 // Per-box FP64 sums of per-tile partials: one block per box, fixed-order tree.
-__global__ void k_reduce_tiles(const int* __restrict__ tile0, const double* __restrict__ tileE,
-                               const double* __restrict__ tileW, double* __restrict__ boxE,
-                               double* __restrict__ boxW) {
-  __shared__ double se[256], sw[256];
-  const int b = blockIdx.x, t0 = tile0[b], t1 = tile0[b + 1];
-  double e = 0.0, w = 0.0;
-  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-    e += tileE[t];
-    w += tileW[t];
+// Per-box sums of per-atom or per-tile values over the boxes' contiguous
+// ranges, in two fixed-order levels so that a box of millions of atoms does
+// not fall on one block: block (c, b) sums chunk c (kRedChunk entries from the
+// box's first one) with a fixed tree, then one block per box sums its chunks
+// in order.  Reproducible bit for bit.  NV = 1 or 2 arrays.
+constexpr int kRedChunk = 4096;
+
+template <typename Off, int NV>
+__global__ void k_chunk_sums(const Off* __restrict__ off, const double* __restrict__ v0,
+                             const double* __restrict__ v1, int maxc, double* __restrict__ partial) {
+  __shared__ double sh[NV][256];
+  const int c = blockIdx.x, b = blockIdx.y;
+  const int64_t a0 = (int64_t)off[b] + (int64_t)c * kRedChunk;
+  const int64_t a1 = min((int64_t)off[b + 1], a0 + kRedChunk);
+  double s0 = 0.0, s1 = 0.0;
+  for (int64_t i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+    s0 += v0[i];
+    if (NV > 1) s1 += v1[i];
   }
-  se[threadIdx.x] = e;
-  sw[threadIdx.x] = w;
+  sh[0][threadIdx.x] = s0;
+  if (NV > 1) sh[NV - 1][threadIdx.x] = s1;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o) {
-      se[threadIdx.x] += se[threadIdx.x + o];
-      sw[threadIdx.x] += sw[threadIdx.x + o];
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+      if (NV > 1) sh[NV - 1][threadIdx.x] += sh[NV - 1][threadIdx.x + o];
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    boxE[b] = se[0];
-    boxW[b] = sw[0];
+    partial[(size_t)b * maxc + c] = sh[0][0];
+    if (NV > 1) partial[((size_t)gridDim.y + b) * maxc + c] = sh[NV - 1][0];
   }
 }
 
-cudaError_t launch_reduce_tiles(int nboxes, const int* tile0, const double* tileE, const double* tileW,
-                                double* boxE, double* boxW, cudaStream_t st) {
-  k_reduce_tiles<<<nboxes, 256, 0, st>>>(tile0, tileE, tileW, boxE, boxW);
+template <int NV>
+__global__ void k_box_sums(const double* __restrict__ partial, int maxc, int nboxes, double* __restrict__ out0,
+                           double* __restrict__ out1) {
+  __shared__ double sh[NV][256];
+  const int b = blockIdx.x;
+  double s0 = 0.0, s1 = 0.0;
+  for (int c = threadIdx.x; c < maxc; c += blockDim.x) {
+    s0 += partial[(size_t)b * maxc + c];
+    if (NV > 1) s1 += partial[((size_t)nboxes + b) * maxc + c];
+  }
+  sh[0][threadIdx.x] = s0;
+  if (NV > 1) sh[NV - 1][threadIdx.x] = s1;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+      if (NV > 1) sh[NV - 1][threadIdx.x] += sh[NV - 1][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out0[b] = sh[0][0];
+    if (NV > 1) out1[b] = sh[NV - 1][0];
+  }
+}
+
+int red_chunks(int64_t max_per_box) { return (int)std::max<int64_t>(1, (max_per_box + kRedChunk - 1) / kRedChunk); }
+
+cudaError_t launch_box_sums(int nboxes, const int64_t* atom0, int maxc, const double* v, double* partial,
+                            double* out, cudaStream_t st) {
+  k_chunk_sums<int64_t, 1><<<dim3(maxc, nboxes), 256, 0, st>>>(atom0, v, nullptr, maxc, partial);
+  k_box_sums<1><<<nboxes, 256, 0, st>>>(partial, maxc, nboxes, out, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_tiles(int nboxes, const int* tile0, int maxc, const double* tileE, const double* tileW,
+                                double* partial, double* boxE, double* boxW, cudaStream_t st) {
+  k_chunk_sums<int, 2><<<dim3(maxc, nboxes), 256, 0, st>>>(tile0, tileE, tileW, maxc, partial);
+  k_box_sums<2><<<nboxes, 256, 0, st>>>(partial, maxc, nboxes, boxE, boxW);
   return cudaGetLastError();
 }
 
@@ -200,7 +247,7 @@ __global__ void k_kick(const KickArgs k) {
 
 cudaError_t launch_kick(const KickArgs& k, cudaStream_t st) {
   if (k.s.N > 0) k_kick<<<(unsigned)((k.s.N + 255) / 256), 256, 0, st>>>(k);
-  if (k.hk > 0.0) k_reduce_atoms<<<k.nboxes, 256, 0, st>>>(k.atom0, k.keAtom, k.boxKE);
+  if (k.hk > 0.0) return launch_box_sums(k.nboxes, k.atom0, k.maxc, k.keAtom, k.partial, k.boxKE, st);
   return cudaGetLastError();
 }
 
@@ -212,11 +259,11 @@ __global__ void k_kinetic(int64_t n, const double* __restrict__ V0, const double
   keAtom[s] = 0.5 * lj.mass[meta[s] & 0xff] * (V0[s] * V0[s] + V1[s] * V1[s] + V2[s] * V2[s]);
 }
 
-cudaError_t launch_kinetic(int64_t n, int nboxes, const int64_t* atom0, const double* const V[3], const int* meta,
-                           LJTable lj, double* keAtom, double* boxKE, cudaStream_t st) {
+cudaError_t launch_kinetic(int64_t n, int nboxes, const int64_t* atom0, int maxc, const double* const V[3],
+                           const int* meta, LJTable lj, double* keAtom, double* partial, double* boxKE,
+                           cudaStream_t st) {
   if (n > 0) k_kinetic<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, V[0], V[1], V[2], meta, lj, keAtom);
-  k_reduce_atoms<<<nboxes, 256, 0, st>>>(atom0, keAtom, boxKE);
-  return cudaGetLastError();
+  return launch_box_sums(nboxes, atom0, maxc, keAtom, partial, boxKE, st);
 }
 
 __global__ void k_scale_v(int64_t n, double* __restrict__ V0, double* __restrict__ V1, double* __restrict__ V2,
