@@ -29,6 +29,7 @@ ERR_CUDA = 206
 ERR_NOMEM = 207
 ERR_STATE = 208
 ERR_NO_DEVICE = 209
+ERR_IO = 210
 
 
 class Params(C.Structure):
@@ -96,6 +97,8 @@ def load():
             "examd_own_table": (C.c_int, [C.POINTER(C.c_byte), C.POINTER(C.c_ubyte)]),
             "examd_host_alloc": (C.c_int, [C.POINTER(vp), C.c_int64]),
             "examd_host_free": (C.c_int, [vp]),
+            "examd_read_particles": (C.c_int, [C.c_char_p, i64p, dp, dp, C.c_int64]),
+            "examd_write_particles": (C.c_int, [C.c_char_p, C.c_int64, dp, dp]),
             "examd_gen_fcc": (C.c_int, [C.c_int, C.c_double, dp, dp]),
             "examd_gen_velocities": (C.c_int, [C.c_int64, ip, dp, C.c_double, C.c_uint64, dp]),
             "examd_gen_random": (C.c_int, [C.c_int64, C.c_int64, dp, dp, dp, C.c_double, C.c_uint64, C.c_int64,
@@ -119,9 +122,8 @@ class ExamdError(RuntimeError):
         self.code = code
 
 
-def check(code: int, where: str = "", ctx=None):
+def check(code: int, where: str = "", ctx=None, detail: str = ""):
     if code != OK:
-        detail = ""
         if ctx is not None and _lib is not None:
             detail = (_lib.examd_gpu_last_error(ctx) or b"").decode()
         raise ExamdError(code, where, detail)

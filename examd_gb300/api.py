@@ -12,6 +12,7 @@ and batched ensembles.  Everything goes through the C ABI of
 from __future__ import annotations
 
 import ctypes as C
+import os
 import weakref
 
 import numpy as np
@@ -211,6 +212,28 @@ def forces_midpoint_all(pos, box, cutoff, eps=1.0, sigma=1.0, forces=None, preci
 
 
 # -- generators (host code in the library) ------------------------------------
+def read_particles(path):
+    """Atoms of an exaMD_particles.dat file (SRC/exaMD_input_formats.f90:128-192): (pos (n, 3), L (3,))."""
+    lib = _L.load()
+    n = C.c_int64()
+    L = np.zeros(3)
+    p = os.fsencode(path)
+    check(lib.examd_read_particles(p, C.byref(n), _d(L), None, 0), "examd_read_particles", detail=str(path))
+    pos = np.zeros((n.value, 3))
+    check(lib.examd_read_particles(p, C.byref(n), _d(L), _d(pos), n.value), "examd_read_particles",
+          detail=str(path))
+    return pos, L
+
+
+def write_particles(path, pos, L):
+    """Write atoms in the exaMD_particles.dat format (exaMD_write_particles, :211-235)."""
+    lib = _L.load()
+    p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    box = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), (3,)))
+    check(lib.examd_write_particles(os.fsencode(path), len(p), _d(box), _d(p)), "examd_write_particles",
+          detail=str(path))
+
+
 def gen_fcc(nc, rho):
     """4*nc^3 atoms on an FCC lattice at density rho; returns (pos (n,3), L)."""
     lib = _L.load()

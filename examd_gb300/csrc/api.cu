@@ -303,6 +303,7 @@ const char* examd_gpu_strerror(int code) {
     case EXAMD_ERR_NOMEM: return "out of device or pinned memory";
     case EXAMD_ERR_STATE: return "invalid call order";
     case EXAMD_ERR_NO_DEVICE: return "no usable sm_103 CUDA device";
+    case EXAMD_ERR_IO: return "file missing, unreadable or malformed";
     default: return "unknown status";
   }
 }

@@ -43,6 +43,7 @@ extern "C" {
 #define EXAMD_ERR_NOMEM 207         /* device or pinned allocation failed     */
 #define EXAMD_ERR_STATE 208         /* call order (e.g. no atoms set)         */
 #define EXAMD_ERR_NO_DEVICE 209     /* no CUDA device / wrong architecture    */
+#define EXAMD_ERR_IO 210            /* file missing, unreadable or malformed  */
 
 #define EXAMD_MAX_TYPES 4
 
@@ -196,6 +197,21 @@ const char *examd_gpu_last_error(examd_ctx *ctx);
 /* Page-locked host buffers for fast copies (cudaHostAlloc). */
 int examd_host_alloc(void **ptr, int64_t bytes);
 int examd_host_free(void *ptr);
+
+/* ---- the reference's particle file (host code, no device use) ----------- */
+
+/* Read exaMD_particles.dat: natms_tot, globalbox(3), then x y z per atom, as
+ * Fortran list-directed records (SRC/exaMD_input_formats.f90:128-192).  With
+ * pos = NULL only *natoms and L[3] are filled; then call again with pos of
+ * capacity >= 3 * natoms doubles.  EXAMD_ERR_IO: missing, short or malformed
+ * file. */
+int examd_read_particles(const char *path, int64_t *natoms, double *L,
+                         double *pos, int64_t capacity);
+
+/* Write the same format (exaMD_write_particles, :211-235) with 17
+ * significant digits, so that the reference reads back the same doubles. */
+int examd_write_particles(const char *path, int64_t natoms, const double *L,
+                          const double *pos);
 
 /* ---- input generators (host code, no device use) ------------------------ */
 
