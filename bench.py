@@ -267,6 +267,7 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=None, help="steps of the energy-drift runs")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 / drift side measurements")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-tune", action="store_true", help="default tile shape instead of the autotuner's")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rk, lr = dist_info()
@@ -289,6 +290,16 @@ def main():
     sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **lj)
     sysm.set_atoms(case["pos"], case["types"], case["vel"])
     equilibrate(sysm, case["natoms"], temps, eq_steps, eq_every, dt)
+    tuning = {"tile": "default", "warps": "default"}
+    if not args.no_tune:
+        # tile edge and warps per CTA for the equilibrated atoms (examd_autotune)
+        pos_eq, vel_eq = sysm.state()
+        tuning = ex.autotune(case["boxes"], case["natoms"], pos_eq, case["types"], precision="mixed", device=lr,
+                             **lj)
+        sysm.close()
+        sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, tile=tuning["tile"],
+                             warps=tuning["warps"], **lj)
+        sysm.set_atoms(pos_eq, case["types"], vel_eq)
     chunk = max(2, args.chunk // 2 * 2)
     wsteps = max(args.warmup, chunk + 2)
     wsteps += wsteps % 2
@@ -369,6 +380,8 @@ def main():
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": label, "atoms": n, "boxes": nboxes, "rc": lj.get("rc"), "dt": dt,
                        "precision": "mixed", "graph_chunk": chunk,
+                       "tile": list(tuning["tile"]) if isinstance(tuning["tile"], tuple) else tuning["tile"],
+                       "warps": tuning["warps"],
                        "l2": "working set > L2 (per-step HBM traffic ~0.2 KB per atom)" if n * 200 > 129e6
                        else "working set fits L2 (small configuration)",
                        "parallelism": f"replicas{ws}"},

@@ -91,6 +91,8 @@ def load():
                                                vp, C.c_char_p, C.c_int]),
             "examd_gpu_scale_velocities": (C.c_int, [ctxp, dp]),
             "examd_gpu_time_forces": (C.c_int, [ctxp, C.c_int, dp, dp]),
+            "examd_autotune": (C.c_int, [C.POINTER(Params), C.c_int, C.POINTER(Box), C.c_int64, dp, ip, C.c_char_p,
+                                         C.POINTER(Params), dp]),
             "examd_gpu_counters": (C.c_int, [ctxp, i64p, i64p, i64p, i64p, i64p]),
             "examd_gpu_strerror": (C.c_char_p, [C.c_int]),
             "examd_gpu_last_error": (C.c_char_p, [ctxp]),

@@ -42,6 +42,58 @@ def _table(v, nt):
     return np.ascontiguousarray(a.reshape(nt, nt))
 
 
+def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None, block_length=None,
+           tile=None, warps=None, strict_box=False, device=0):
+    """examd_params and the examd_box array of a system, from Python arguments."""
+    lib = _L.load()
+    b = np.atleast_2d(np.asarray(boxes, dtype=np.float64))
+    n = np.atleast_1d(np.asarray(natoms, dtype=np.int64))
+    if b.shape[1] != 3 or b.shape[0] != n.shape[0]:
+        raise ValueError("boxes must be (nboxes, 3) with one natoms per box")
+    if precision not in (FP64, MIXED):
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    p = _L.Params()
+    lib.examd_default_params(C.byref(p))
+    p.precision = _L.FP64 if precision == FP64 else _L.MIXED
+    p.ntypes = int(ntypes)
+    e, s, r = _table(eps, ntypes), _table(sigma, ntypes), _table(rc, ntypes)
+    for k in range(ntypes * ntypes):
+        p.eps[k] = e.flat[k]
+        p.sigma[k] = s.flat[k]
+        p.rc[k] = r.flat[k]
+    m = np.ones(ntypes) if mass is None else np.broadcast_to(np.asarray(mass, dtype=np.float64), (ntypes,))
+    for k in range(ntypes):
+        p.mass[k] = m[k]
+    p.cell_edge = 0.0 if block_length is None else float(block_length)
+    if tile is not None:
+        for a in range(3):
+            p.tile[a] = int(tile[a] if np.ndim(tile) else tile)
+    p.warps = 0 if warps is None else int(warps)
+    p.strict_box = 1 if strict_box else 0
+    p.device = int(device)
+    arr = (_L.Box * b.shape[0])()
+    for k in range(b.shape[0]):
+        for a in range(3):
+            arr[k].L[a] = b[k, a]
+        arr[k].natoms = int(n[k])
+    return lib, p, arr, b, n, np.array(m, dtype=np.float64)
+
+
+def autotune(boxes, natoms, pos, types=None, cache=None, **kw):
+    """Tile edge and warps per CTA for this system, picked by timing the pair
+    kernel on these atoms (examd_autotune).  cache: path of a text cache of
+    earlier choices, or None.  Returns dict(tile, warps, ms per launch)."""
+    lib, p, arr, b, n, _ = _setup(boxes, natoms, **kw)
+    pp = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    t = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
+    best = _L.Params()
+    ms = C.c_double()
+    path = None if cache is None else os.fsencode(cache)
+    check(lib.examd_autotune(C.byref(p), len(n), arr, len(pp), _d(pp), _i(t), path, C.byref(best), C.byref(ms)),
+          "examd_autotune")
+    return {"tile": tuple(int(v) for v in best.tile), "warps": int(best.warps), "ms": ms.value}
+
+
 class MidpointLJ:
     """Resident GPU state for one box or a batch of independent boxes.
 
@@ -53,50 +105,32 @@ class MidpointLJ:
 
     def __init__(self, boxes, natoms, *, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None,
                  block_length=None, tile=None, warps=None, strict_box=False, device=0):
-        lib = _L.load()
+        lib, p, arr, b, n, m = _setup(boxes, natoms, precision, eps, sigma, rc, ntypes, mass, block_length, tile,
+                                      warps, strict_box, device)
         self._lib = lib
-        b = np.atleast_2d(np.asarray(boxes, dtype=np.float64))
-        n = np.atleast_1d(np.asarray(natoms, dtype=np.int64))
-        if b.shape[1] != 3 or b.shape[0] != n.shape[0]:
-            raise ValueError("boxes must be (nboxes, 3) with one natoms per box")
         self.nboxes = int(b.shape[0])
         self.natoms = n.copy()
         self.n = int(n.sum())
         self.box_edges = b.copy()
-        p = _L.Params()
-        lib.examd_default_params(C.byref(p))
-        p.precision = _L.FP64 if precision == FP64 else _L.MIXED
-        if precision not in (FP64, MIXED):
-            raise ValueError("precision must be 'fp64' or 'mixed'")
         self.precision = precision
-        p.ntypes = int(ntypes)
-        e, s, r = _table(eps, ntypes), _table(sigma, ntypes), _table(rc, ntypes)
-        for k in range(ntypes * ntypes):
-            p.eps[k] = e.flat[k]
-            p.sigma[k] = s.flat[k]
-            p.rc[k] = r.flat[k]
-        m = np.ones(ntypes) if mass is None else np.broadcast_to(np.asarray(mass, dtype=np.float64), (ntypes,))
-        for k in range(ntypes):
-            p.mass[k] = m[k]
-        self.mass = np.array(m, dtype=np.float64)
-        p.cell_edge = 0.0 if block_length is None else float(block_length)
-        if tile is not None:
-            for a in range(3):
-                p.tile[a] = int(tile[a] if np.ndim(tile) else tile)
-        p.warps = 0 if warps is None else int(warps)
-        p.strict_box = 1 if strict_box else 0
-        p.device = int(device)
+        self.mass = m
         self.params = p
-        arr = (_L.Box * self.nboxes)()
-        for k in range(self.nboxes):
-            for a in range(3):
-                arr[k].L[a] = b[k, a]
-            arr[k].natoms = int(n[k])
         ctx = C.c_void_p()
         check(lib.examd_gpu_create(C.byref(p), self.nboxes, arr, C.byref(ctx)), "examd_gpu_create")
         self._ctx = ctx
         self._fin = weakref.finalize(self, lib.examd_gpu_destroy, ctx)
         self.types = None
+        self.tuning = None
+
+    @classmethod
+    def tuned(cls, boxes, natoms, pos, types=None, vel=None, cache=None, **kw):
+        """A system whose tile shape and CTA width the autotuner picked for these atoms."""
+        r = autotune(boxes, natoms, pos, types, cache, **kw)
+        kw = dict(kw, tile=r["tile"], warps=r["warps"])
+        s = cls(boxes, natoms, **kw)
+        s.set_atoms(pos, types, vel)
+        s.tuning = r
+        return s
 
     # -- lifecycle -----------------------------------------------------------
     def close(self):

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_lib", "obj")
 LIB = os.path.join(OUT_DIR, "libexamd_gb300.so")
-SOURCES = ["api.cu", "bin.cu", "pair.cu", "step.cu", "static_kinetic.cu", "gen.cpp", "io.cpp"]
+SOURCES = ["api.cu", "bin.cu", "pair.cu", "step.cu", "static_kinetic.cu", "gen.cpp", "io.cpp", "tune.cpp"]
 HEADERS = ["common.cuh", "kernels.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1,0 +1,125 @@
+// tune.cpp -- the tile shape and CTA width of the pair kernel, picked per
+// system by timing.
+//
+// The reference has no counterpart: its work decomposition is the METIS
+// partition of the block graph (SRC/exaMD_partitioning.f90), fixed by the
+// process count.  Here the unit of work is a CTA tile of home cells; its edge
+// (3-6 cells) trades halo overhead against shared memory per CTA and CTAs per
+// SM, and the warps per CTA trade latency hiding against tail imbalance.  The
+// cell edge stays at the reference's rc/2: a larger edge only adds candidate
+// pairs, and a smaller one breaks the 63-entry table.
+//
+// Each candidate gets its own context on the caller's atoms; the pair kernel
+// is timed with CUDA events (one warm-up launch, then kReps launches).  A
+// candidate that does not fit (capacity, memory) is skipped.  Choices can be
+// kept in a text cache keyed by device, precision, types, cutoff, box count,
+// atom count and density.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/examd_gb300.h"
+
+namespace {
+
+constexpr int kReps = 3;
+
+std::string cache_key(const examd_params& p, int nboxes, const examd_box* boxes, int64_t n) {
+  cudaDeviceProp pr;
+  std::string dev = "unknown";
+  if (cudaGetDeviceProperties(&pr, p.device) == cudaSuccess)
+    dev = std::string(pr.name) + "/" + std::to_string(pr.multiProcessorCount);
+  for (char& c : dev)
+    if (c == ' ') c = '_';
+  double vol = 0.0, rcmax = 0.0;
+  for (int b = 0; b < nboxes; ++b) vol += boxes[b].L[0] * boxes[b].L[1] * boxes[b].L[2];
+  for (int k = 0; k < p.ntypes * p.ntypes; ++k) rcmax = std::fmax(rcmax, p.rc[k]);
+  char buf[256];
+  // atom count in quarter-octaves, density to 0.05
+  std::snprintf(buf, sizeof buf, "%s|%s|nt%d|rc%.4g|boxes%d|n%.2f|rho%.2f", dev.c_str(),
+                p.precision == EXAMD_FP64 ? "fp64" : "mixed", p.ntypes, rcmax, nboxes,
+                std::round(std::log2((double)(n > 0 ? n : 1)) * 4.0) / 4.0, std::round(n / vol * 20.0) / 20.0);
+  return buf;
+}
+
+bool cache_lookup(const char* path, const std::string& key, int tile[3], int* warps, double* ms) {
+  if (!path) return false;
+  std::FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char line[512];
+  bool hit = false;
+  while (std::fgets(line, sizeof line, f)) {
+    char* sep = std::strrchr(line, '|');
+    if (!sep || (size_t)(sep - line) != key.size() || std::strncmp(line, key.c_str(), key.size()) != 0) continue;
+    int t0, t1, t2, w;
+    double m;
+    if (std::sscanf(sep + 1, "%d %d %d %d %lf", &t0, &t1, &t2, &w, &m) == 5) {
+      tile[0] = t0;
+      tile[1] = t1;
+      tile[2] = t2;
+      *warps = w;
+      *ms = m;
+      hit = true;  // the last entry wins
+    }
+  }
+  std::fclose(f);
+  return hit;
+}
+
+// The key's fields are joined by '|'; the choice follows the last '|'.
+void cache_store(const char* path, const std::string& key, const int tile[3], int warps, double ms) {
+  if (!path) return;
+  std::FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f, "%s|%d %d %d %d %.17g\n", key.c_str(), tile[0], tile[1], tile[2], warps, ms);
+  std::fclose(f);
+}
+
+}  // namespace
+
+extern "C" int examd_autotune(const examd_params* params, int nboxes, const examd_box* boxes, int64_t n,
+                              const double* pos, const int* type, const char* cache_path, examd_params* best,
+                              double* best_ms) {
+  if (!params || !boxes || nboxes < 1 || n < 0 || (n > 0 && !pos) || !best) return EXAMD_ERR_ARG;
+  const std::string key = cache_key(*params, nboxes, boxes, n);
+  examd_params out = *params;
+  double ms = 0.0;
+  if (cache_lookup(cache_path, key, out.tile, &out.warps, &ms)) {
+    *best = out;
+    if (best_ms) *best_ms = ms;
+    return EXAMD_OK;
+  }
+  const int edges[] = {3, 4, 5, 6};
+  const int widths[] = {8, 4};
+  double best_t = INFINITY;
+  int last_rc = EXAMD_ERR_CELL_OVERFLOW;
+  for (int e : edges)
+    for (int w : widths) {
+      examd_params p = *params;
+      p.tile[0] = p.tile[1] = p.tile[2] = e;
+      p.warps = w;
+      examd_ctx* ctx = nullptr;
+      int rc = examd_gpu_create(&p, nboxes, boxes, &ctx);
+      double t = 0.0;
+      if (rc == EXAMD_OK) rc = examd_gpu_set_atoms(ctx, n, pos, type, nullptr);
+      if (rc == EXAMD_OK) rc = examd_gpu_time_forces(ctx, kReps, nullptr, &t);
+      if (ctx) examd_gpu_destroy(ctx);
+      if (rc == EXAMD_ERR_NO_DEVICE || rc == EXAMD_ERR_ARG || rc == EXAMD_ERR_OUTSIDE) return rc;
+      if (rc != EXAMD_OK) {
+        last_rc = rc;
+        continue;
+      }
+      if (t < best_t) {
+        best_t = t;
+        out = p;
+      }
+    }
+  if (!std::isfinite(best_t)) return last_rc;
+  cache_store(cache_path, key, out.tile, out.warps, best_t);
+  *best = out;
+  if (best_ms) *best_ms = best_t;
+  return EXAMD_OK;
+}

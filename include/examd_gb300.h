@@ -165,6 +165,18 @@ int examd_kinetic_static(int device, int64_t natoms, int nboxes,
 /* Scale all velocities of box b by factor[b] (thermostat / melt protocol). */
 int examd_gpu_scale_velocities(examd_ctx *ctx, const double *factor);
 
+/* Autotuner (no counterpart in the reference, whose decomposition is the
+ * METIS partition): time the pair kernel on these atoms for tile edges of 3-6
+ * home cells and 4 or 8 warps per CTA, and return the fastest in *best (a copy
+ * of *params with tile and warps set) and its time per launch in *best_ms.
+ * cache_path (may be NULL): a text file of earlier choices keyed by device,
+ * precision, types, cutoff, box count, atom count and density; a hit returns
+ * without timing, a miss is appended.  pos/type as in examd_gpu_set_atoms. */
+int examd_autotune(const examd_params *params, int nboxes,
+                   const examd_box *boxes, int64_t n, const double *pos,
+                   const int *type, const char *cache_path,
+                   examd_params *best, double *best_ms);
+
 /* Device time in ms of `reps` force evaluations (positions already resident),
  * measured with CUDA events on the context's stream.  kernel_ms, when
  * non-NULL, receives the average duration of the pair kernel alone. */
