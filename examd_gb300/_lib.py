@@ -30,6 +30,8 @@ ERR_NOMEM = 207
 ERR_STATE = 208
 ERR_NO_DEVICE = 209
 ERR_IO = 210
+ERR_PAIRFN = 211
+POT_LJ, POT_LJ_SHIFTED, POT_WCA = 0, 1, 2
 
 
 class Params(C.Structure):
@@ -45,6 +47,7 @@ class Params(C.Structure):
         ("warps", C.c_int),
         ("strict_box", C.c_int),
         ("device", C.c_int),
+        ("potential", C.c_int),
     ]
 
 

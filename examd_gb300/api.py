@@ -42,8 +42,11 @@ def _table(v, nt):
     return np.ascontiguousarray(a.reshape(nt, nt))
 
 
+POTENTIALS = {"lj": _L.POT_LJ, "lj_shifted": _L.POT_LJ_SHIFTED, "wca": _L.POT_WCA}
+
+
 def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None, block_length=None,
-           tile=None, warps=None, strict_box=False, device=0):
+           tile=None, warps=None, strict_box=False, device=0, potential="lj"):
     """examd_params and the examd_box array of a system, from Python arguments."""
     lib = _L.load()
     b = np.atleast_2d(np.asarray(boxes, dtype=np.float64))
@@ -71,6 +74,9 @@ def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, 
     p.warps = 0 if warps is None else int(warps)
     p.strict_box = 1 if strict_box else 0
     p.device = int(device)
+    if potential not in POTENTIALS:
+        raise ValueError(f"potential must be one of {sorted(POTENTIALS)}")
+    p.potential = POTENTIALS[potential]
     arr = (_L.Box * b.shape[0])()
     for k in range(b.shape[0]):
         for a in range(3):
@@ -101,12 +107,13 @@ class MidpointLJ:
     precision: "fp64" (FP64 end to end) or "mixed" (FP32 pair forces, FP64
     positions, integration and reductions).  eps/sigma/rc: scalars or
     (ntypes, ntypes) tables; block_length defaults to max(rc)/2 as the
-    reference (exaMD.f90:56)."""
+    reference (exaMD.f90:56).  potential: the pair function, "lj" (the
+    reference's lennardjones_12), "lj_shifted" or "wca"."""
 
     def __init__(self, boxes, natoms, *, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None,
-                 block_length=None, tile=None, warps=None, strict_box=False, device=0):
+                 block_length=None, tile=None, warps=None, strict_box=False, device=0, potential="lj"):
         lib, p, arr, b, n, m = _setup(boxes, natoms, precision, eps, sigma, rc, ntypes, mass, block_length, tile,
-                                      warps, strict_box, device)
+                                      warps, strict_box, device, potential)
         self._lib = lib
         self.nboxes = int(b.shape[0])
         self.natoms = n.copy()

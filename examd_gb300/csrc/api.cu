@@ -239,6 +239,7 @@ void free_all(examd_ctx* ctx) {
 }
 
 int status_to_code(int st) {
+  if (st & ST_PAIRFN) return EXAMD_ERR_PAIRFN;
   if (st & ST_NONFINITE) return EXAMD_ERR_NONFINITE;
   if (st & ST_OUTSIDE) return EXAMD_ERR_OUTSIDE;
   if (st & ST_OVERFLOW) return EXAMD_ERR_CELL_OVERFLOW;
@@ -304,6 +305,7 @@ const char* examd_gpu_strerror(int code) {
     case EXAMD_ERR_STATE: return "invalid call order";
     case EXAMD_ERR_NO_DEVICE: return "no usable sm_103 CUDA device";
     case EXAMD_ERR_IO: return "file missing, unreadable or malformed";
+    case EXAMD_ERR_PAIRFN: return "the pair function returned an error (e.g. coincident atoms)";
     default: return "unknown status";
   }
 }
@@ -333,6 +335,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   const examd_params& p = *params;
   if (p.ntypes < 1 || p.ntypes > EXAMD_MAX_TYPES) return EXAMD_ERR_ARG;
   if (p.precision != EXAMD_FP64 && p.precision != EXAMD_MIXED) return EXAMD_ERR_ARG;
+  if (p.potential < EXAMD_POT_LJ || p.potential > EXAMD_POT_WCA) return EXAMD_ERR_ARG;
   const int nt = p.ntypes;
   double rcmax = 0.0;
   for (int a = 0; a < nt; ++a)
@@ -387,16 +390,34 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   LJTable& lj = ctx->lj;
   lj.nt = nt;
   float rc2max = 0.f;
+  lj.pot = p.potential;
   for (int k = 0; k < nt * nt; ++k) {
     const double e = p.eps[k], s = p.sigma[k], r = p.rc[k];
     lj.p64[k].sig2 = s * s;      // sig2 = prmvdw(1,2)**2   (user_func.f90:59)
     lj.p64[k].eps24 = 24.0 * e;  // eps24 = twentyfour*eps  (user_func.f90:58)
     lj.p64[k].eps4 = 4.0 * e;
     lj.p64[k].rc2 = r * r;       // prmvdw(1,5)**2           (user_func.f90:52)
+    // the potential's own range and energy shift
+    double rcut2 = r * r, eshift = 0.0;
+    if (p.potential == EXAMD_POT_LJ_SHIFTED) {
+      const double s6 = std::pow(s * s / (r * r), 3);
+      eshift = 4.0 * e * s6 * (s6 - 1.0);
+    } else if (p.potential == EXAMD_POT_WCA) {
+      rcut2 = std::cbrt(2.0) * s * s;  // (2^(1/6) sigma)^2
+      eshift = -e;                     // U(2^(1/6) sigma) = -eps
+      if (rcut2 > r * r) {  // rc must cover the potential's range
+        delete ctx;
+        return EXAMD_ERR_ARG;
+      }
+    }
+    lj.p64[k].rcut2 = rcut2;
+    lj.p64[k].eshift = eshift;
     lj.p32[k].sig2 = (float)(s * s);
     lj.p32[k].m24eps = (float)(-24.0 * e);
     lj.p32[k].c4eps = (float)(4.0 * e);
     lj.p32[k].rc2 = (float)(r * r);
+    lj.p32[k].rcut2 = (float)rcut2;
+    lj.p32[k].eshift = (float)eshift;
     rc2max = std::max(rc2max, lj.p32[k].rc2);
   }
   lj.rc2max = rc2max;

@@ -32,6 +32,7 @@ enum StatusBits : int {
   ST_NONFINITE = 2,  // NaN / Inf position
   ST_OUTSIDE = 4,    // position outside [0,L) in strict mode
   ST_TIMEOUT = 8,    // a bounded wait gave up
+  ST_PAIRFN = 16,    // the pair function returned an error
 };
 
 struct BoxDev {
@@ -47,15 +48,20 @@ struct BoxDev {
 };
 
 // LJ parameters per ordered type pair, FP32 (mixed) and FP64.
+// rc2: the candidate cutoff (distance test, queue); rcut2: the potential's
+// own range (<= rc2); eshift: subtracted from the pair energy.
 struct LJ32 {
   float sig2, m24eps, c4eps, rc2;  // m24eps = -24 eps (dg prefactor)
+  float rcut2, eshift;
 };
 struct LJ64 {
   double sig2, eps24, eps4, rc2;   // as user_func.f90:58-59 computes them
+  double rcut2, eshift;
 };
 
 struct LJTable {
   int nt;
+  int pot;       // EXAMD_POT_*
   float rc2max;
   float prune2;  // (max rc + 1e-4)^2: cell boxes farther than this hold no pair
   LJ32 p32[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];

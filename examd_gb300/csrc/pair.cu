@@ -37,6 +37,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "pairfn.cuh"
 
 namespace examd {
 
@@ -120,9 +121,9 @@ struct FixSum {
 // (a segmented shuffle scan; integer sums, so the result is exact) and the
 // run's last lane adds the total: one shared atomic per run instead of one
 // per pair on the same address.
-template <bool MULTI, bool ENERGY>
+template <bool MULTI, bool ENERGY, bool COUNT>
 __device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int* qk, int* fa, float* fr, int cap,
-                                            const LJTable& lj, FixSum& ek, FixSum& wk) {
+                                            const LJTable& lj, FixSum& ek, FixSum& wk, int* status, int& nacc) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const bool act = lane < cnt;
@@ -135,17 +136,20 @@ __device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int
     m = (key >> 14) & 0x3fff;
     LJ32 P = lj.p32[0];
     if (MULTI) P = lj.p32[((key >> 28) & 3) * lj.nt + (key >> 30)];
-    const float ri = rcp_approx(d.w);
-    const float s2 = P.sig2 * ri;
-    const float s6 = s2 * s2 * s2;
-    const float dg = P.m24eps * s6 * fmaf(2.f, s6, -1.f) * ri;
-    const float dgs = kFix * dg;
-    fx = dgs * d.x;
-    fy = dgs * d.y;
-    fz = dgs * d.z;
-    if (ENERGY) {
-      ek.add(P.c4eps * s6 * (s6 - 1.f));
-      wk.add(-dg * d.w);
+    float dg = 0.f, e = 0.f;
+    const int rv = pair_fn32<ENERGY>(lj.pot, d.w, P, dg, e);
+    if (rv == 0) {
+      const float dgs = kFix * dg;
+      fx = dgs * d.x;
+      fy = dgs * d.y;
+      fz = dgs * d.z;
+      if (ENERGY) {
+        ek.add(e);
+        wk.add(-dg * d.w);
+      }
+      if (COUNT) ++nacc;
+    } else if (rv < 0) {
+      atomicOr(status, ST_PAIRFN);
     }
   }
   // terms too large for the fixed-point sums take the FP32 side path
@@ -196,7 +200,8 @@ __device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int
 template <bool MULTI, bool ENERGY, bool COUNT>
 __device__ __forceinline__ void force_batch64(int cnt, const int* qk, const double* pd, const unsigned short* code,
                                               const signed char* img, const double* Lbox, double* fd, int cap,
-                                              const LJTable& lj, double& esum, double& wsum, int& nacc) {
+                                              const LJTable& lj, double& esum, double& wsum, int* status,
+                                              int& nacc) {
   const int lane = threadIdx.x & 31;
   if (lane >= cnt) return;
   const unsigned key = (unsigned)qk[lane];
@@ -215,12 +220,9 @@ __device__ __forceinline__ void force_batch64(int cnt, const int* qk, const doub
   const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
   LJ64 P = lj.p64[0];
   if (MULTI) P = lj.p64[((key >> 28) & 3) * lj.nt + (key >> 30)];
-  if (d2 <= P.rc2) {
-    const double d2i = __drcp_rn(d2);
-    const double tt = __dmul_rn(P.sig2, d2i);
-    const double d6 = __dmul_rn(__dmul_rn(tt, tt), tt);
-    const double d12 = __dmul_rn(d6, d6);
-    const double dg = -__dmul_rn(__dmul_rn(P.eps24, __dsub_rn(__dmul_rn(2.0, d12), d6)), d2i);
+  double dg = 0.0, e = 0.0;
+  const int rv = pair_fn64<ENERGY>(lj.pot, d2, P, dg, e);
+  if (rv == 0) {
     const double fx = __dmul_rn(dg, dx), fy = __dmul_rn(dg, dy), fz = __dmul_rn(dg, dz);
     atomicAdd(&fd[i], fx);
     atomicAdd(&fd[cap + i], fy);
@@ -229,10 +231,12 @@ __device__ __forceinline__ void force_batch64(int cnt, const int* qk, const doub
     atomicAdd(&fd[cap + m], -fy);
     atomicAdd(&fd[2 * cap + m], -fz);
     if (ENERGY) {
-      esum += __dmul_rn(P.eps4, __dsub_rn(d12, d6));
+      esum += e;
       wsum += -__dmul_rn(dg, d2);
     }
     if (COUNT) ++nacc;
+  } else if (rv < 0) {
+    atomicOr(status, ST_PAIRFN);
   }
 }
 
@@ -479,15 +483,15 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
         const int p = qn + __popc(bal & lt);
         if (!FP64) qd[p] = dq;
         qk[p] = kb | (m << 14) | (tj << 30);
-        if (!FP64 && COUNT) ++nacc;
       }
       qn += __popc(bal);
       if (qn >= 32) {
         __syncwarp();
         if (FP64)
-          force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, nacc);
+          force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status,
+                                              nacc);
         else
-          force_batch<MULTI, ENERGY>(32, qd, qk, fa, fr, cap, A.lj, ek, wk);
+          force_batch<MULTI, ENERGY, COUNT>(32, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
         __syncwarp();
         const int rem = qn - 32;
         float4 kd = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -622,9 +626,9 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   if (qn > 0) {  // the last, partial batch
     __syncwarp();
     if (FP64)
-      force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, nacc);
+      force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc);
     else
-      force_batch<MULTI, ENERGY>(qn, qd, qk, fa, fr, cap, A.lj, ek, wk);
+      force_batch<MULTI, ENERGY, COUNT>(qn, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
   }
   __syncthreads();
 

@@ -44,8 +44,20 @@ extern "C" {
 #define EXAMD_ERR_STATE 208         /* call order (e.g. no atoms set)         */
 #define EXAMD_ERR_NO_DEVICE 209     /* no CUDA device / wrong architecture    */
 #define EXAMD_ERR_IO 210            /* file missing, unreadable or malformed  */
+#define EXAMD_ERR_PAIRFN 211        /* the pair function returned an error    */
 
 #define EXAMD_MAX_TYPES 4
+
+/* Pair functions (examd_params.potential), the counterpart of the reference's
+ * External :: user_func (SRC/exaMD_forces.f90:532) and its return codes: 0
+ * apply the pair, > 0 skip it, < 0 error (EXAMD_ERR_PAIRFN; coincident atoms,
+ * r^2 < 1e-12, are an error for every potential). */
+#define EXAMD_POT_LJ 0         /* lennardjones_12 (user_func.f90:40-75): cut at
+                                  rc, unshifted; energy 4 eps (s^12 - s^6)   */
+#define EXAMD_POT_LJ_SHIFTED 1 /* same forces, energy shifted to 0 at rc     */
+#define EXAMD_POT_WCA 2        /* LJ cut at 2^(1/6) sigma and shifted up by
+                                  eps (purely repulsive); rc only bounds the
+                                  candidate pairs and must be >= that range  */
 
 /* Precision forms. */
 #define EXAMD_FP64 0  /* FP64 end to end                                       */
@@ -73,6 +85,7 @@ typedef struct examd_params {
   int strict_box;     /* 1: positions outside [0,L) are an error (109);       */
                       /* 0: they are wrapped periodically                     */
   int device;         /* CUDA device ordinal                                  */
+  int potential;      /* EXAMD_POT_*                                          */
 } examd_params;
 
 /* One independent periodic box of a batched ensemble. */
