@@ -175,6 +175,7 @@ struct examd_ctx {
   int64_t* d_atom0 = nullptr;
   double* keAtom = nullptr;
   double* partial = nullptr;  // chunk partial sums of the per-box reductions
+  int* h_status = nullptr;    // pinned host copy of the status word
   int maxc_atoms = 1, maxc_tiles = 1;
   int ebuf_steps = 0;
 
@@ -231,6 +232,7 @@ void free_all(examd_ctx* ctx) {
     if (ctx->meta[b]) cudaFree(ctx->meta[b]);
     if (ctx->id[b]) cudaFree(ctx->id[b]);
   }
+  if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->e0) cudaEventDestroy(ctx->e0);
   if (ctx->e1) cudaEventDestroy(ctx->e1);
   if (ctx->e2) cudaEventDestroy(ctx->e2);
@@ -542,6 +544,13 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     delete ctx;
     return EXAMD_ERR_CUDA;
   }
+  if (cudaHostAlloc((void**)&ctx->h_status, sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+    ctx->h_status = nullptr;
+    free_all(ctx);
+    delete ctx;
+    return EXAMD_ERR_NOMEM;
+  }
+  *ctx->h_status = 0;
   const size_t N = (size_t)ctx->N, NC = (size_t)ctx->NC;
   ALLOC(ctx->d_boxes, nboxes);
   ALLOC(ctx->d_tiles, tiles.size());
@@ -665,15 +674,25 @@ int finish_binning(examd_ctx* ctx) {
   return EXAMD_OK;
 }
 
-int check_status(examd_ctx* ctx) {
-  int h = 0;
-  CK(cudaMemcpyAsync(&h, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
-  CK(cudaStreamSynchronize(ctx->st));
+// The status word after work already synchronised: its copy to the pinned
+// host word was queued before that synchronisation (queue_status).
+int take_status(examd_ctx* ctx) {
+  const int h = *ctx->h_status;
   if (h) {
     CK(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
   }
   return status_to_code(h);
+}
+
+cudaError_t queue_status(examd_ctx* ctx) {
+  return cudaMemcpyAsync(ctx->h_status, ctx->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st);
+}
+
+int check_status(examd_ctx* ctx) {
+  CK(queue_status(ctx));
+  CK(cudaStreamSynchronize(ctx->st));
+  return take_status(ctx);
 }
 
 // Staged-atom capacity of a tile from the current binning (+25% + 64 headroom).
@@ -764,8 +783,9 @@ int forces_common(examd_ctx* ctx, double* forces, double* epot, double* virial, 
   }
   if (epot) CK(cudaMemcpyAsync(epot, ctx->boxE, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (virial) CK(cudaMemcpyAsync(virial, ctx->boxW, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(queue_status(ctx));
   CK(cudaStreamSynchronize(st));
-  rc = check_status(ctx);
+  rc = take_status(ctx);
   if (rc) return rc;
   ctx->forces_valid = true;
   return EXAMD_OK;

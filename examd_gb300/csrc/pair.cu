@@ -122,16 +122,18 @@ struct FixSum {
 // run's last lane adds the total: one shared atomic per run instead of one
 // per pair on the same address.
 template <bool MULTI, bool ENERGY, bool COUNT>
-__device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int* qk, int* fa, float* fr, int cap,
-                                            const LJTable& lj, FixSum& ek, FixSum& wk, int* status, int& nacc) {
+__device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, const int* qk, int* fa, float* fr,
+                                            int cap, const LJTable& lj, FixSum& ek, FixSum& wk, int* status,
+                                            int& nacc) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const bool act = lane < cnt;
   int i = -1, m = 0;
   float fx = 0.f, fy = 0.f, fz = 0.f;
   if (act) {
-    const float4 d = qd[lane];
-    const unsigned key = (unsigned)qk[lane];
+    const int slot = (qh + lane) & (kQueue - 1);
+    const float4 d = qd[slot];
+    const unsigned key = (unsigned)qk[slot];
     i = key & 0x3fff;
     m = (key >> 14) & 0x3fff;
     LJ32 P = lj.p32[0];
@@ -171,12 +173,14 @@ __device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int
     atomicAdd(&fr[cap + m], -fy * kFixInv);
     atomicAdd(&fr[2 * cap + m], -fz * kFixInv);
   }
-  // i side: sum over runs of equal i (inactive lanes form one run with i = -1)
+  // i side: sum over runs of equal i (inactive lanes form one run with i = -1),
+  // in segments of 8 lanes from the run's first one: each segment's last lane
+  // adds the segment's total
   const int ip = __shfl_up_sync(FULL, i, 1);
   const unsigned hb = __ballot_sync(FULL, lane == 0 || ip != i);
-  const int dist = lane - (31 - __clz(hb & (FULL >> (31 - lane))));
+  const int dist = (lane - (31 - __clz(hb & (FULL >> (31 - lane))))) & 7;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
+  for (int o = 1; o < 8; o <<= 1) {
     const int yx = __shfl_up_sync(FULL, ix, o), yy = __shfl_up_sync(FULL, iy, o), yz = __shfl_up_sync(FULL, iz, o);
     if (o <= dist) {
       ix += yx;
@@ -184,7 +188,7 @@ __device__ __forceinline__ void force_batch(int cnt, const float4* qd, const int
       iz += yz;
     }
   }
-  const bool tail = lane == 31 || ((hb >> (lane + 1)) & 1u);
+  const bool tail = lane == 31 || dist == 7 || ((hb >> (lane + 1)) & 1u);
   if (act && tail) {
     atomicAdd(&fa[i], ix);
     atomicAdd(&fa[cap + i], iy);
@@ -201,10 +205,10 @@ template <bool MULTI, bool ENERGY, bool COUNT>
 __device__ __forceinline__ void force_batch64(int cnt, const int* qk, const double* pd, const unsigned short* code,
                                               const signed char* img, const double* Lbox, double* fd, int cap,
                                               const LJTable& lj, double& esum, double& wsum, int* status,
-                                              int& nacc) {
+                                              int& nacc, int qh) {
   const int lane = threadIdx.x & 31;
   if (lane >= cnt) return;
-  const unsigned key = (unsigned)qk[lane];
+  const unsigned key = (unsigned)qk[(qh + lane) & (kQueue - 1)];
   const int i = key & 0x3fff, m = (key >> 14) & 0x3fff;
   const int ci = code[i], cm = code[m];
   // difference of the copies' periodic images per axis: -1, 0 or +1 box
@@ -415,7 +419,7 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   int* qk = (int*)(smem + L.queue + kQd * kQueue * nw) + warp * kQueue;
   // per-warp table of one step's items: (C, key base)
   float4* ptA = (float4*)(smem + L.queue + (kQd + 4) * kQueue * nw) + warp * 32;
-  int qn = 0;
+  int qn = 0, qh = 0;  // queued pairs and the ring's head
   const unsigned lt = (1u << lane) - 1u;
   const unsigned le = FULL >> (31 - lane);
   unsigned char* r2l = smem + L.r2l + 64 * warp;  // two rank -> lane tables of 32
@@ -480,33 +484,21 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
       const bool acc = valid && dq.w <= thr;
       const unsigned bal = __ballot_sync(FULL, acc);
       if (acc) {
-        const int p = qn + __popc(bal & lt);
+        const int p = (qh + qn + __popc(bal & lt)) & (kQueue - 1);
         if (!FP64) qd[p] = dq;
         qk[p] = kb | (m << 14) | (tj << 30);
       }
       qn += __popc(bal);
-      if (qn >= 32) {
+      if (qn >= 32) {  // the queue is a ring: a batch only moves its head
         __syncwarp();
         if (FP64)
           force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status,
-                                              nacc);
+                                              nacc, qh);
         else
-          force_batch<MULTI, ENERGY, COUNT>(32, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
+          force_batch<MULTI, ENERGY, COUNT>(32, qh, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
         __syncwarp();
-        const int rem = qn - 32;
-        float4 kd = make_float4(0.f, 0.f, 0.f, 0.f);
-        int kk = 0;
-        if (lane < rem) {
-          if (!FP64) kd = qd[32 + lane];
-          kk = qk[32 + lane];
-        }
-        __syncwarp();
-        if (lane < rem) {
-          if (!FP64) qd[lane] = kd;
-          qk[lane] = kk;
-        }
-        qn = rem;
-        __syncwarp();
+        qh = (qh + 32) & (kQueue - 1);
+        qn -= 32;
       }
     }
     __syncwarp();
@@ -626,9 +618,10 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   if (qn > 0) {  // the last, partial batch
     __syncwarp();
     if (FP64)
-      force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc);
+      force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
+                                          qh);
     else
-      force_batch<MULTI, ENERGY, COUNT>(qn, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
+      force_batch<MULTI, ENERGY, COUNT>(qn, qh, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
   }
   __syncthreads();
 
