@@ -47,6 +47,7 @@ cudaError_t upload_own_lut(const OwnLut& lut) { return cudaMemcpyToSymbol(c_own,
 
 constexpr int kDT = 6;        // origin differences for d = -2..3
 constexpr int kQueue = 64;    // per-warp queue of accepted pairs
+constexpr int kParts = 2;     // work units per 32 staged atoms (1, 3 and 4 measured slower)
 constexpr float kFix = 32768.f;        // fixed-point scale 2^15
 constexpr float kFixInv = 1.f / 32768.f;
 constexpr float kFixMax = 1024.f;      // larger terms take the FP32 side path
@@ -505,16 +506,16 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   };
 
   // ---- item building: (staged atom, owned row) pairs, laid end to end ----
-  // A unit is 32 consecutive staged atoms and one half of each atom's list of
-  // owned rows (the rows whose ownership mask for the atom's position class is
-  // nonzero; ordinals n = 2m + half).  The warp lays the unit's (atom, row)
-  // pairs end to end and builds one item per lane per step, so lanes do not
-  // idle on atoms that own few rows (the halo).  Units are handed out by a
+  // A unit is 32 consecutive staged atoms and one of kParts shares of each
+  // atom's list of owned rows (the rows whose ownership mask for the atom's
+  // position class is nonzero; ordinals n = kParts m + part).  The warp lays
+  // the unit's (atom, row) pairs end to end and builds one item per lane per
+  // step, so lanes do not idle on atoms that own few rows (the halo).  Units are handed out by a
   // shared counter: their cost varies, and the force sums do not depend on the
   // order.  An item is the atom's j-range(s) in the row: the owned cells,
   // trimmed to those whose box comes within rc of the atom (the 1e-4 margin in
   // prune2 covers the FP32 rounding; the accepted pairs are unchanged).
-  const int nunits = 2 * ((total + 31) >> 5);
+  const int nunits = kParts * ((total + 31) >> 5);
   const float prune2 = A.lj.prune2;
   int* ucnt = (int*)(red + 8 * nw);
   while (true) {
@@ -522,14 +523,14 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
     if (lane == 0) u = atomicAdd(ucnt, 1);
     u = __shfl_sync(FULL, u, 0);
     if (u >= nunits) break;
-    const int c = u >> 1, half = u & 1;
+    const int c = u / kParts, part = u - c * kParts;
     // per-atom quantities of lane l's atom c*32 + l
     const int ia = c * 32 + lane;
     const bool va = ia < total;
     const int cia = code[va ? ia : 0];
     const int ax = cia & 31, ay = (cia >> 5) & 31, az = cia >> 10;
     const int acls = pos_class(ax - 1, tx) * 25 + pos_class(ay - 1, ty) * 5 + pos_class(az - 1, tz);
-    const int aw = va ? (sown->nrow[acls] + 1 - half) >> 1 : 0;
+    const int aw = va ? (sown->nrow[acls] + kParts - 1 - part) / kParts : 0;
     const float4 pa = pf[va ? ia : 0];
     const float apy = FP64 ? pa.y : oy[ay] + pa.y;  // tile-frame y, z
     const float apz = FP64 ? pa.z : oz[az] + pa.z;
@@ -565,7 +566,7 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
       const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
       int r = 0, mask = 0;
       if (valid) {
-        r = sown->rlist[cls][2 * (k - s_q) + half];
+        r = sown->rlist[cls][kParts * (k - s_q) + part];
         mask = sown->lut[cls][r];
       }
       int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
