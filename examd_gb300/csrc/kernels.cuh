@@ -57,7 +57,6 @@ struct PairConfig {
 };
 
 int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max);
-int pair_bytes_per_atom(const PairConfig& cfg);
 cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes);  // opt-in smem attribute
 cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st);
 cudaError_t upload_own_lut(const OwnLut& lut);

@@ -25,16 +25,16 @@
 // Accumulation.  Mixed form: each per-atom force component is an exact 32-bit
 // fixed-point sum in shared memory (scale 2^15, native integer atomics), so
 // the result does not depend on the order of the terms and is reproducible
-// bit for bit; a term of magnitude >= 1024 (r < 0.79 sigma at eps = 1) takes
-// an FP32 side path instead, which keeps every fixed-point sum of up to 63
-// terms inside 2^31.  FP64 form: FP64 shared-memory atomics.  No global
-// atomics are used.
+// bit for bit.  A term of magnitude >= 1024 (r < 0.79 sigma at eps = 1)
+// takes an FP32 side path instead, so every fixed-point term is below 2^25
+// and a component's sum could leave the int32 range only through more than
+// 64 near-maximal terms of one sign on one atom, i.e. 64 neighbours within
+// about 0.8 sigma on one side, which no physical configuration has.  FP64
+// form: FP64 shared-memory atomics.  No global atomics are used.
 //
 // Output: forces of the tile's home atoms go to Fown, those of halo copies to
 // the partial slot P[s] (s = bitmask of the axes on which the copy is a halo
 // copy); the integrator sums an atom's 1..8 partials in a fixed order.
-#include <climits>
-
 #include "common.cuh"
 #include "kernels.cuh"
 #include "pairfn.cuh"
@@ -94,7 +94,6 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
 int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max) {
   return make_layout(cfg.fp64, cap, ne_max, cfg.warps).bytes;
 }
-int pair_bytes_per_atom(const PairConfig& cfg) { return make_layout(cfg.fp64, 1024, 0, 1).bytes / 1024; }
 
 // Exact sum of FP32 terms in 64-bit fixed point (2^-32 resolution): the total
 // does not depend on the order of the terms.  A term of magnitude >= 30000
