@@ -120,6 +120,9 @@ int round_block_length(double want, double* out, int* q_out, int* k_out) {
 
 }  // namespace
 
+constexpr int kIoChunks = 4;            // host <-> device transfers of the force call, in chunks
+constexpr int64_t kIoMinChunk = 1 << 16;  // atoms; smaller calls use fewer chunks
+
 struct examd_ctx {
   examd_params p{};
   int nboxes = 0;
@@ -176,6 +179,11 @@ struct examd_ctx {
   double* keAtom = nullptr;
   double* partial = nullptr;  // chunk partial sums of the per-box reductions
   int* h_status = nullptr;    // pinned host copy of the status word
+  // caller-order I/O in chunks, copies on a second stream
+  int* inv = nullptr;         // caller index -> sorted slot
+  bool inv_valid = false;     // inv matches the current sorted order
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_io[3 * kIoChunks + 1] = {};
   int maxc_atoms = 1, maxc_tiles = 1;
   int ebuf_steps = 0;
 
@@ -233,6 +241,10 @@ void free_all(examd_ctx* ctx) {
     if (ctx->id[b]) cudaFree(ctx->id[b]);
   }
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
+  if (ctx->inv) cudaFree(ctx->inv);
+  for (cudaEvent_t e : ctx->ev_io)
+    if (e) cudaEventDestroy(e);
+  if (ctx->st2) cudaStreamDestroy(ctx->st2);
   if (ctx->e0) cudaEventDestroy(ctx->e0);
   if (ctx->e1) cudaEventDestroy(ctx->e1);
   if (ctx->e2) cudaEventDestroy(ctx->e2);
@@ -551,6 +563,13 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     return EXAMD_ERR_NOMEM;
   }
   *ctx->h_status = 0;
+  bool io_ok = cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) == cudaSuccess;
+  for (cudaEvent_t& e : ctx->ev_io) io_ok = io_ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  if (!io_ok) {
+    free_all(ctx);
+    delete ctx;
+    return EXAMD_ERR_CUDA;
+  }
   const size_t N = (size_t)ctx->N, NC = (size_t)ctx->NC;
   ALLOC(ctx->d_boxes, nboxes);
   ALLOC(ctx->d_tiles, tiles.size());
@@ -601,6 +620,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   ALLOC(ctx->d_factor, nboxes);
   ALLOC(ctx->d_atom0, nboxes + 1);
   ALLOC(ctx->keAtom, N);
+  ALLOC(ctx->inv, N);
   {
     int64_t maxa = 1, maxt = 1;
     for (int b = 0; b < nboxes; ++b) {
@@ -650,7 +670,8 @@ namespace {
 inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
 
 // Scan, place and final ordering after a counting pass; swaps the buffers.
-int finish_binning(examd_ctx* ctx) {
+// want_inv: also record the caller -> sorted map (for the caller-order I/O).
+int finish_binning(examd_ctx* ctx, bool want_inv) {
   cudaStream_t st = ctx->st;
   const int nc = ctx->NC;
   const int nsb = (nc + kScanTileHost - 1) / kScanTileHost;
@@ -665,13 +686,30 @@ int finish_binning(examd_ctx* ctx) {
                                               ctx->V[s][1], ctx->V[s][2], ctx->meta[s], ctx->id[s],
                                               ctx->X[d][0], ctx->X[d][1], ctx->X[d][2], ctx->V[d][0],
                                               ctx->V[d][1], ctx->V[d][2], ctx->meta[d], ctx->id[d], ctx->U,
-                                              ctx->cellS);
+                                              ctx->cellS, want_inv ? ctx->inv : nullptr);
   } else {
     k_place<<<1, 32, 0, st>>>(0, nc, ctx->cellOld, ctx->slot, ctx->cstart, ctx->src);
   }
   CK(cudaGetLastError());
   ctx->cur = d;
+  ctx->inv_valid = want_inv;
   return EXAMD_OK;
+}
+
+// Chunk c of n atoms for the caller-order I/O: [i0, i1).
+int io_chunks(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(kIoChunks, n / kIoMinChunk)); }
+void io_range(int64_t n, int nch, int c, int64_t& i0, int64_t& i1) {
+  i0 = n * c / nch;
+  i1 = n * (c + 1) / nch;
+}
+
+// The caller -> sorted map of the current order, if the last binning did not
+// record it.
+cudaError_t ensure_inv(examd_ctx* ctx) {
+  if (ctx->inv_valid || ctx->N == 0) return cudaSuccess;
+  k_inverse<<<nblk(ctx->N), 256, 0, ctx->st>>>(ctx->N, ctx->id[ctx->cur], ctx->inv);
+  ctx->inv_valid = true;
+  return cudaGetLastError();
 }
 
 // The status word after work already synchronised: its copy to the pinned
@@ -771,19 +809,46 @@ StepArgs step_args(examd_ctx* ctx) {
   return s;
 }
 
+// The pair path at the resident positions, then the forces to the caller in
+// chunks of its own order: the device->host copy of chunk c (second stream)
+// overlaps the gather of chunk c + 1.  With accumulate, the caller's forces
+// come in on the second stream while the pair kernel runs.
 int forces_common(examd_ctx* ctx, double* forces, double* epot, double* virial, int accumulate) {
-  cudaStream_t st = ctx->st;
+  cudaStream_t st = ctx->st, st2 = ctx->st2;
   const bool energy = epot || virial;
+  const int64_t N = ctx->N;
+  const int nch = io_chunks(N);
+  cudaEvent_t* ev_acc = ctx->ev_io + 2 * kIoChunks;
+  if (forces && accumulate && N > 0) {
+    CK(cudaEventRecord(ctx->ev_io[3 * kIoChunks], st));  // stage is free once earlier work is done
+    CK(cudaStreamWaitEvent(st2, ctx->ev_io[3 * kIoChunks], 0));
+    for (int c = 0; c < nch; ++c) {
+      int64_t i0, i1;
+      io_range(N, nch, c, i0, i1);
+      CK(cudaMemcpyAsync(ctx->stage + 3 * i0, forces + 3 * i0, 3 * (i1 - i0) * sizeof(double),
+                         cudaMemcpyHostToDevice, st2));
+      CK(cudaEventRecord(ev_acc[c], st2));
+    }
+  }
   int rc = run_pair(ctx, energy, false);
   if (rc) return rc;
-  if (forces) {
-    if (accumulate) CK(cudaMemcpyAsync(ctx->stage, forces, 3 * ctx->N * sizeof(double), cudaMemcpyHostToDevice, st));
-    CK(launch_forces_out(step_args(ctx), ctx->id[ctx->cur], ctx->stage, accumulate, st));
-    CK(cudaMemcpyAsync(forces, ctx->stage, 3 * ctx->N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (forces && N > 0) {
+    CK(ensure_inv(ctx));
+    for (int c = 0; c < nch; ++c) {
+      int64_t i0, i1;
+      io_range(N, nch, c, i0, i1);
+      if (accumulate) CK(cudaStreamWaitEvent(st, ev_acc[c], 0));
+      CK(launch_forces_out(step_args(ctx), i0, i1, ctx->inv, ctx->stage, accumulate, st));
+      CK(cudaEventRecord(ctx->ev_io[kIoChunks + c], st));
+      CK(cudaStreamWaitEvent(st2, ctx->ev_io[kIoChunks + c], 0));
+      CK(cudaMemcpyAsync(forces + 3 * i0, ctx->stage + 3 * i0, 3 * (i1 - i0) * sizeof(double),
+                         cudaMemcpyDeviceToHost, st2));
+    }
   }
   if (epot) CK(cudaMemcpyAsync(epot, ctx->boxE, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (virial) CK(cudaMemcpyAsync(virial, ctx->boxW, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(queue_status(ctx));
+  CK(cudaStreamSynchronize(st2));
   CK(cudaStreamSynchronize(st));
   rc = take_status(ctx);
   if (rc) return rc;
@@ -820,7 +885,7 @@ int examd_gpu_set_atoms(examd_ctx* ctx, int64_t n, const double* pos, const int*
                                         ctx->slot, ctx->Uold, ctx->count, ctx->status);
     CK(cudaGetLastError());
   }
-  int rc = finish_binning(ctx);
+  int rc = finish_binning(ctx, true);
   if (rc) return rc;
   CK(cudaStreamSynchronize(st));
   rc = check_status(ctx);
@@ -844,17 +909,31 @@ int examd_gpu_forces_at(examd_ctx* ctx, const double* pos, double* forces, doubl
   if (!ctx || (ctx->N > 0 && !pos)) return EXAMD_ERR_ARG;
   if (!ctx->atoms_set) return EXAMD_ERR_STATE;
   cudaSetDevice(ctx->dev);
-  cudaStream_t st = ctx->st;
+  cudaStream_t st = ctx->st, st2 = ctx->st2;
   const int s = ctx->cur;
-  if (ctx->N > 0) {
-    CK(cudaMemcpyAsync(ctx->stage2, pos, 3 * ctx->N * sizeof(double), cudaMemcpyHostToDevice, st));
-    k_gather_pos_bin<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, ctx->stage2, ctx->d_boxes, ctx->p.strict_box,
-                                                   ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->meta[s],
-                                                   ctx->id[s], ctx->cellOld, ctx->slot, ctx->Uold, ctx->count,
-                                                   ctx->status);
-    CK(cudaGetLastError());
+  const int64_t N = ctx->N;
+  if (N > 0) {
+    // positions in chunks of the caller's order: the host->device copy of
+    // chunk c + 1 (second stream) overlaps the gather and binning count of chunk c
+    CK(ensure_inv(ctx));
+    CK(cudaEventRecord(ctx->ev_io[3 * kIoChunks], st));
+    CK(cudaStreamWaitEvent(st2, ctx->ev_io[3 * kIoChunks], 0));
+    const int nch = io_chunks(N);
+    for (int c = 0; c < nch; ++c) {
+      int64_t i0, i1;
+      io_range(N, nch, c, i0, i1);
+      CK(cudaMemcpyAsync(ctx->stage2 + 3 * i0, pos + 3 * i0, 3 * (i1 - i0) * sizeof(double),
+                         cudaMemcpyHostToDevice, st2));
+      CK(cudaEventRecord(ctx->ev_io[c], st2));
+      CK(cudaStreamWaitEvent(st, ctx->ev_io[c], 0));
+      k_gather_pos_bin_range<<<nblk(i1 - i0), 256, 0, st>>>(i0, i1, ctx->stage2, ctx->d_boxes, ctx->p.strict_box,
+                                                            ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->meta[s],
+                                                            ctx->inv, ctx->cellOld, ctx->slot, ctx->Uold, ctx->count,
+                                                            ctx->status);
+      CK(cudaGetLastError());
+    }
   }
-  int rc = finish_binning(ctx);
+  int rc = finish_binning(ctx, true);
   if (rc) return rc;
   return forces_common(ctx, forces, epot, virial, accumulate);
 }
@@ -900,7 +979,7 @@ KickArgs kick_args(examd_ctx* ctx, double ckick, double dt, bool drift, double h
 int step_once(examd_ctx* ctx, double ck, double dt, double* keSlot, double* eSlot, double* wSlot) {
   const double h = 0.5 * dt;
   CK(launch_kick(kick_args(ctx, ck, dt, true, keSlot ? h : 0.0, keSlot), ctx->st));
-  int rc = finish_binning(ctx);
+  int rc = finish_binning(ctx, false);
   if (rc) return rc;
   return run_pair(ctx, eSlot != nullptr, false, eSlot, wSlot);
 }

@@ -65,18 +65,19 @@ __global__ void k_load_bin(int64_t n, const double* __restrict__ aos, const doub
   bin_one((int)s, p[0], p[1], p[2], mt, boxes, cellOld, slot, Uold, count, status);
 }
 
-// New positions in caller order (AoS) for atoms already held in sorted order:
-// gather by id, wrap, bin.
-__global__ void k_gather_pos_bin(int64_t n, const double* __restrict__ aos, const BoxDev* __restrict__ boxes,
-                                 int strict, double* __restrict__ X0, double* __restrict__ X1,
-                                 double* __restrict__ X2, const int* __restrict__ meta,
-                                 const int* __restrict__ id, int* __restrict__ cellOld, int* __restrict__ slot,
-                                 float4* __restrict__ Uold, int* __restrict__ count, int* __restrict__ status) {
-  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  int mt = meta[s];
+// New positions for the caller's atoms [i0, i1) (AoS, caller order, as they
+// arrive in chunks): wrap, store at the atom's sorted slot inv[i], bin.
+__global__ void k_gather_pos_bin_range(int64_t i0, int64_t i1, const double* __restrict__ aos,
+                                       const BoxDev* __restrict__ boxes, int strict, double* __restrict__ X0,
+                                       double* __restrict__ X1, double* __restrict__ X2,
+                                       const int* __restrict__ meta, const int* __restrict__ inv,
+                                       int* __restrict__ cellOld, int* __restrict__ slot, float4* __restrict__ Uold,
+                                       int* __restrict__ count, int* __restrict__ status) {
+  const int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= i1) return;
+  const int s = inv[i];
+  const int mt = meta[s];
   const BoxDev& B = boxes[mt >> 8];
-  int64_t i = id[s];
   double p[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -87,7 +88,7 @@ __global__ void k_gather_pos_bin(int64_t n, const double* __restrict__ aos, cons
   X0[s] = p[0];
   X1[s] = p[1];
   X2[s] = p[2];
-  bin_one((int)s, p[0], p[1], p[2], mt, boxes, cellOld, slot, Uold, count, status);
+  bin_one(s, p[0], p[1], p[2], mt, boxes, cellOld, slot, Uold, count, status);
 }
 
 // Bin the current positions without moving them (after a velocity-only change
@@ -210,7 +211,8 @@ __global__ void k_finalize(int64_t n, const int* __restrict__ src, const int* __
                            const int* __restrict__ meta, const int* __restrict__ id, double* __restrict__ Y0,
                            double* __restrict__ Y1, double* __restrict__ Y2, double* __restrict__ W0,
                            double* __restrict__ W1, double* __restrict__ W2, int* __restrict__ meta2,
-                           int* __restrict__ id2, float4* __restrict__ U, int* __restrict__ cellS) {
+                           int* __restrict__ id2, float4* __restrict__ U, int* __restrict__ cellS,
+                           int* __restrict__ inv) {
   int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (j >= n) return;
   int s = src[j];
@@ -230,6 +232,13 @@ __global__ void k_finalize(int64_t n, const int* __restrict__ src, const int* __
   id2[d] = myid;
   U[d] = Uold[s];
   cellS[d] = c;
+  if (inv) inv[myid] = d;  // caller index -> sorted slot, when the caller's order is needed next
+}
+
+// inv[id[s]] = s: the caller-order map of the current sorted order.
+__global__ void k_inverse(int64_t n, const int* __restrict__ id, int* __restrict__ inv) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s < n) inv[id[s]] = (int)s;
 }
 
 }  // namespace examd

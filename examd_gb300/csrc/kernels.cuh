@@ -10,9 +10,10 @@ __global__ void k_load_bin(int64_t n, const double* aos, const double* vaos, con
                            const BoxDev* boxes, int strict, double* X0, double* X1, double* X2, double* V0,
                            double* V1, double* V2, int* meta, int* id, int* cellOld, int* slot, float4* Uold,
                            int* count, int* status);
-__global__ void k_gather_pos_bin(int64_t n, const double* aos, const BoxDev* boxes, int strict, double* X0,
-                                 double* X1, double* X2, const int* meta, const int* id, int* cellOld, int* slot,
-                                 float4* Uold, int* count, int* status);
+__global__ void k_gather_pos_bin_range(int64_t i0, int64_t i1, const double* aos, const BoxDev* boxes, int strict,
+                                       double* X0, double* X1, double* X2, const int* meta, const int* inv,
+                                       int* cellOld, int* slot, float4* Uold, int* count, int* status);
+__global__ void k_inverse(int64_t n, const int* id, int* inv);
 __global__ void k_bin(int64_t n, const double* X0, const double* X1, const double* X2, const int* meta,
                       const BoxDev* boxes, int* cellOld, int* slot, float4* Uold, int* count, int* status);
 __global__ void k_scan_reduce(int nc, const int* count, int* bsum);
@@ -23,7 +24,7 @@ __global__ void k_finalize(int64_t n, const int* src, const int* cellOld, const 
                            const double* X0, const double* X1, const double* X2, const double* V0,
                            const double* V1, const double* V2, const int* meta, const int* id, double* Y0,
                            double* Y1, double* Y2, double* W0, double* W1, double* W2, int* meta2, int* id2,
-                           float4* U, int* cellS);
+                           float4* U, int* cellS, int* inv);
 constexpr int kScanTileHost = 2048;  // cells per scan block (kScanThreads * kScanItems)
 
 // ---- pair.cu ----------------------------------------------------------------
@@ -73,7 +74,8 @@ struct StepArgs {
 };
 
 // F = Fown + halo partials, in caller order, AoS doubles (out[3*id + a]); += if accumulate.
-cudaError_t launch_forces_out(const StepArgs& s, const int* id, double* out, int accumulate, cudaStream_t st);
+cudaError_t launch_forces_out(const StepArgs& s, int64_t i0, int64_t i1, const int* inv, double* out, int accumulate,
+                              cudaStream_t st);
 // Per-box sums of the per-tile energy/virial partials (FP64, fixed order).
 // Per-box sums in two fixed-order levels (chunks of 4096 entries, then the
 // box's chunks in order); partial holds nboxes * maxc doubles (tiles: twice).

@@ -73,12 +73,14 @@ __device__ __forceinline__ void gather_force(const StepArgs& a, int64_t s, doubl
   }
 }
 
-__global__ void k_forces_out(const StepArgs a, const int* __restrict__ id, double* __restrict__ out, int acc) {
-  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= a.N) return;
+// Forces of the caller's atoms [i0, i1) in caller order (AoS): the atom's
+// partials gathered at its sorted slot inv[i]; written or added (acc).
+__global__ void k_forces_out(const StepArgs a, int64_t i0, int64_t i1, const int* __restrict__ inv,
+                             double* __restrict__ out, int acc) {
+  const int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= i1) return;
   double f[3];
-  gather_force(a, s, f);
-  int64_t i = id[s];
+  gather_force(a, inv[i], f);
   if (acc) {
     out[3 * i] += f[0];
     out[3 * i + 1] += f[1];
@@ -90,9 +92,10 @@ __global__ void k_forces_out(const StepArgs a, const int* __restrict__ id, doubl
   }
 }
 
-cudaError_t launch_forces_out(const StepArgs& s, const int* id, double* out, int accumulate, cudaStream_t st) {
-  if (s.N == 0) return cudaSuccess;
-  k_forces_out<<<(unsigned)((s.N + 255) / 256), 256, 0, st>>>(s, id, out, accumulate);
+cudaError_t launch_forces_out(const StepArgs& s, int64_t i0, int64_t i1, const int* inv, double* out, int accumulate,
+                              cudaStream_t st) {
+  if (i1 <= i0) return cudaSuccess;
+  k_forces_out<<<(unsigned)((i1 - i0 + 255) / 256), 256, 0, st>>>(s, i0, i1, inv, out, accumulate);
   return cudaGetLastError();
 }
 
