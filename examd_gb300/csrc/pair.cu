@@ -19,8 +19,11 @@
 // of one step (at most 32) have their candidate pairs laid end to end and
 // tested 32 at a time, one per lane.  Accepted pairs are queued and their
 // forces computed in batches of 32, both atoms' sums updated (Newton's third
-// law).  The FP64 form tests the candidates with an FP32 prefilter on a
-// widened cutoff and computes the queued pairs in FP64.
+// law).  The FP64 form builds items per (ext cell, row) instead: the block
+// of the cell's atoms against the row's owned j-cells, untrimmed, tested with
+// an FP32 prefilter on a widened cutoff; the queued pairs are computed in
+// FP64.  Its batches then hold pairs of many different i atoms, so their FP64
+// shared-memory atomics (the FP64 form's bound) rarely hit one address.
 //
 // Accumulation.  Mixed form: each per-atom force component is an exact 32-bit
 // fixed-point sum in shared memory (scale 2^15, native integer atomics), so
@@ -267,7 +270,6 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   signed char* img = (signed char*)(smem + L.img);
   double* red = (double*)(smem + L.red);
   OwnLut* sown = (OwnLut*)(smem + L.lut);
-  const unsigned char* slut = &sown->lut[0][0];
   const signed char* srows = &sown->rows[0][0];
   float4* pf = (float4*)(smem + L.pf);
   unsigned short* code = (unsigned short*)(smem + L.code);
@@ -407,7 +409,6 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   __syncthreads();
 
   const LJ32 q32 = A.lj.p32[0];
-  const LJ64 q64 = A.lj.p64[0];
   const float rcpre = A.lj.rc2max * 1.0001f + 1e-4f;  // FP32 prefilter of the FP64 form
   double esum = 0.0, wsum = 0.0;  // FP64 form
   FixSum ek, wk;                  // mixed form: exact fixed-point sums of FP32 terms
@@ -424,12 +425,34 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   const unsigned le = FULL >> (31 - lane);
   unsigned char* r2l = smem + L.r2l + 64 * warp;  // two rank -> lane tables of 32
 
-  // ---- consume one step's items, at most one per lane (nt = 0: none) ----
-  // Mixed form: the items' candidate pairs are laid end to end and the warp
-  // walks them 32 at a time, one pair per lane, so no lane idles while another
-  // finishes a long j-range.  A lane finds its item from the bitmask of the
-  // items that start in the current 32 candidates.  FP64 form: each lane walks
-  // its own item's j-ranges.
+  // ---- accepted pairs go to the warp's queue (a ring of kQueue entries);
+  // their forces are computed in full batches of 32 ----
+  auto enqueue = [&](bool acc, const float4& dq, int key) {
+    const unsigned bal = __ballot_sync(FULL, acc);
+    if (acc) {
+      const int p = (qh + qn + __popc(bal & lt)) & (kQueue - 1);
+      if (!FP64) qd[p] = dq;
+      qk[p] = key;
+    }
+    qn += __popc(bal);
+    if (qn >= 32) {  // a batch only moves the ring's head
+      __syncwarp();
+      if (FP64)
+        force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
+                                            qh);
+      else
+        force_batch<MULTI, ENERGY, COUNT>(32, qh, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
+      __syncwarp();
+      qh = (qh + 32) & (kQueue - 1);
+      qn -= 32;
+    }
+  };
+
+  // ---- mixed form: consume one step's (atom, row) items, at most one per
+  // lane (nt = 0: none).  The items' candidate pairs are laid end to end and
+  // the warp walks them 32 at a time, one pair per lane, so no lane idles
+  // while another finishes a long j-range.  A lane finds its item from the
+  // bitmask of the items that start in the current 32 candidates.
   auto consume = [&](int i, int r, int lo1, int n1, int lo2, int n2) {
     const int nt = n1 + n2;
     const unsigned hb = __ballot_sync(FULL, nt > 0);
@@ -446,19 +469,18 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
     const int p1 = lo1 | (n1 << 16), l2 = lo2 - n1;
     if (nt > 0) {
       // the atom's position moved into the j-cells' frame: d = x_j + C
-      // (mixed: y, z relative to the cell origin; FP64: tile frame)
+      // (y, z relative to the cell origin)
       const float4 pi = pf[i];
       const int ci = code[i];
       const int ly = (ci >> 5) & 31, lz = ci >> 10;
       const int dy = srows[2 * r], dz = srows[2 * r + 1];
-      const float Cy = FP64 ? -pi.y : dyt[ly * kDT + dy + 2] - pi.y;
-      const float Cz = FP64 ? -pi.z : dzt[lz * kDT + dz + 2] - pi.z;
+      const float Cy = dyt[ly * kDT + dy + 2] - pi.y;
+      const float Cz = dzt[lz * kDT + dz + 2] - pi.z;
       ptA[lane] = make_float4(-pi.x, Cy, Cz, __int_as_float(i | (__float_as_int(pi.w) << 28)));
       r2l[32 + __popc(hb & lt)] = (unsigned char)lane;
     }
     __syncwarp();
-    // distance tests (FP64 form: the FP32 prefilter); accepted pairs go to the
-    // warp's queue and their forces are computed in full batches of 32
+    // distance tests; accepted pairs go to the queue
     int qb = 0;  // items that start before K
     for (int K = 0; K < T; K += 32) {
       const unsigned M = __reduce_or_sync(FULL, (nt > 0 && (unsigned)(s0 - K) < 32u) ? 1u << (s0 - K) : 0u);
@@ -480,113 +502,249 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
       const int tj = __float_as_int(pj.w);
       const int kb = __float_as_int(a.w);
       if (COUNT && valid) ++neval;
-      const float thr = FP64 ? rcpre : (MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2);
-      const bool acc = valid && dq.w <= thr;
-      const unsigned bal = __ballot_sync(FULL, acc);
-      if (acc) {
-        const int p = (qh + qn + __popc(bal & lt)) & (kQueue - 1);
-        if (!FP64) qd[p] = dq;
-        qk[p] = kb | (m << 14) | (tj << 30);
-      }
-      qn += __popc(bal);
-      if (qn >= 32) {  // the queue is a ring: a batch only moves its head
-        __syncwarp();
-        if (FP64)
-          force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status,
-                                              nacc, qh);
-        else
-          force_batch<MULTI, ENERGY, COUNT>(32, qh, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
-        __syncwarp();
-        qh = (qh + 32) & (kQueue - 1);
-        qn -= 32;
-      }
+      const float thr = MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
+      enqueue(valid && dq.w <= thr, dq, kb | (m << 14) | (tj << 30));
     }
     __syncwarp();
   };
 
-  // ---- item building: (staged atom, owned row) pairs, laid end to end ----
-  // A unit is 32 consecutive staged atoms and one of kParts shares of each
-  // atom's list of owned rows (the rows whose ownership mask for the atom's
-  // position class is nonzero; ordinals n = kParts m + part).  The warp lays
-  // the unit's (atom, row) pairs end to end and builds one item per lane per
-  // step, so lanes do not idle on atoms that own few rows (the halo).  Units are handed out by a
-  // shared counter: their cost varies, and the force sums do not depend on the
-  // order.  An item is the atom's j-range(s) in the row: the owned cells,
-  // trimmed to those whose box comes within rc of the atom (the 1e-4 margin in
-  // prune2 covers the FP32 rounding; the accepted pairs are unchanged).
-  const int nunits = kParts * ((total + 31) >> 5);
-  const float prune2 = A.lj.prune2;
-  int* ucnt = (int*)(red + 8 * nw);
-  while (true) {
-    int u = 0;
-    if (lane == 0) u = atomicAdd(ucnt, 1);
-    u = __shfl_sync(FULL, u, 0);
-    if (u >= nunits) break;
-    const int c = u / kParts, part = u - c * kParts;
-    // per-atom quantities of lane l's atom c*32 + l
-    const int ia = c * 32 + lane;
-    const bool va = ia < total;
-    const int cia = code[va ? ia : 0];
-    const int ax = cia & 31, ay = (cia >> 5) & 31, az = cia >> 10;
-    const int acls = pos_class(ax - 1, tx) * 25 + pos_class(ay - 1, ty) * 5 + pos_class(az - 1, tz);
-    const int aw = va ? (sown->nrow[acls] + kParts - 1 - part) / kParts : 0;
-    const float4 pa = pf[va ? ia : 0];
-    const float apy = FP64 ? pa.y : oy[ay] + pa.y;  // tile-frame y, z
-    const float apz = FP64 ? pa.z : oz[az] + pa.z;
-    // squared x-gaps to the cells dx = -2, -1, +1, +2 (ox has EX + 1 entries)
-    const float gm2 = fmaxf(pa.x - ox[max(ax - 1, 0)], 0.f), gm1 = fmaxf(pa.x - ox[ax], 0.f);
-    const float gp1 = fmaxf(ox[min(ax + 1, EX)] - pa.x, 0.f), gp2 = fmaxf(ox[min(ax + 2, EX)] - pa.x, 0.f);
-    const float am2 = gm2 * gm2, am1 = gm1 * gm1, ap1 = gp1 * gp1, ap2 = gp2 * gp2;
-    int incl = aw;
+  // ---- FP64 form: consume one step's (ext cell, row) blocks ----
+  // Item (at most one per lane): atoms [i0, i0 + ni) of one cell against the
+  // j-range(s) [lo1, lo1 + n1) and [lo2, lo2 + n2) of one owned row; in the
+  // row through the cell itself (self) only j > i.  The items' ni * nj
+  // candidate pairs are laid end to end and tested 32 at a time, one per lane,
+  // against the FP32 prefilter.  A lane finds its item from the bitmask of
+  // item starts and splits its index into (i, j) by a float division
+  // corrected to the exact quotient.  Consecutive queued pairs then share an
+  // i only within one block (a few pairs), which keeps the FP64 batches'
+  // shared-memory atomics on i from serialising; the atom-item order of the
+  // mixed form would put one atom's whole row list (~30 pairs) in a batch.
+  auto consume_cells = [&](int i0, int ni, int lo1, int n1, int lo2, int n2, bool self) {
+    const int nj = n1 + n2;
+    const int nt = ni * nj;
+    const unsigned hb = __ballot_sync(FULL, nt > 0);
+    if (hb == 0u) return;
+    int incl = nt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int y = __shfl_up_sync(FULL, incl, o);
       if (lane >= o) incl += y;
     }
-    const int as0 = incl - aw, W = __shfl_sync(FULL, incl, 31);
-    const unsigned wb = __ballot_sync(FULL, aw > 0);
-    if (aw > 0) r2l[__popc(wb & lt)] = (unsigned char)lane;
+    const int s0 = incl - nt;
+    const int T = __shfl_sync(FULL, incl, 31);
+    const int pa = i0 | (ni << 16), p1 = lo1 | (n1 << 16), l2 = lo2 - n1, pn = nj | (self ? 1 << 16 : 0);
+    if (nt > 0) {
+      ptA[lane] = make_float4(0.f, 0.f, 1.0f / (float)nj, __int_as_float(s0));
+      r2l[32 + __popc(hb & lt)] = (unsigned char)lane;
+    }
     __syncwarp();
-    int qb = 0;  // working atoms that start before K
-    for (int K = 0; K < W; K += 32) {
-      const unsigned M = __reduce_or_sync(FULL, (aw > 0 && (unsigned)(as0 - K) < 32u) ? 1u << (as0 - K) : 0u);
-      const int qr = qb + __popc(M & (FULL >> (31 - lane))) - 1;  // >= 0: the first worker starts at 0
+    int qb = 0;  // items that start before K
+    for (int K = 0; K < T; K += 32) {
+      const unsigned M = __reduce_or_sync(FULL, (nt > 0 && (unsigned)(s0 - K) < 32u) ? 1u << (s0 - K) : 0u);
+      const int qr = qb + __popc(M & le) - 1;  // >= 0: the first item starts at 0
       qb += __popc(M);
+      const int ql = r2l[32 + qr];
+      const int bpa = __shfl_sync(FULL, pa, ql), bp1 = __shfl_sync(FULL, p1, ql);
+      const int bl2 = __shfl_sync(FULL, l2, ql), bpn = __shfl_sync(FULL, pn, ql);
+      const float4 a = ptA[ql];
       const int k = K + lane;
-      const bool valid = k < W;
-      const int ql = r2l[qr];
-      const int s_q = __shfl_sync(FULL, as0, ql);
-      const int ci = __shfl_sync(FULL, cia, ql);
-      const int cls = __shfl_sync(FULL, acls, ql);
-      const float py = __shfl_sync(FULL, apy, ql), pz = __shfl_sync(FULL, apz, ql);
-      const float xm2 = __shfl_sync(FULL, am2, ql), xm1 = __shfl_sync(FULL, am1, ql);
-      const float xp1 = __shfl_sync(FULL, ap1, ql), xp2 = __shfl_sync(FULL, ap2, ql);
-      const int i = c * 32 + ql;
-      const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
-      int r = 0, mask = 0;
-      if (valid) {
-        r = sown->rlist[cls][kParts * (k - s_q) + part];
-        mask = sown->lut[cls][r];
+      const int kl = k - __float_as_int(a.w);
+      const int bnj = bpn & 0xffff;
+      int ia = __float2int_rz(((float)kl + 0.5f) * a.z);
+      int jb = kl - ia * bnj;
+      if (jb < 0) {
+        --ia;
+        jb += bnj;
+      } else if (jb >= bnj) {
+        ++ia;
+        jb -= bnj;
       }
-      int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
-      if (mask) {
-        const int dy = srows[2 * r], dz = srows[2 * r + 1];
-        const int rowbase = ((ly + dy) + EY * (lz + dz)) * EX + lx - 2;  // + bit b -> ext cell of dx = b - 2
-        if (COUNT) {  // every atom of the owned cells, as the reference visits them
-          for (int b = 0; b < 5; ++b)
-            if ((mask >> b) & 1) {
-              const int e = rowbase + b;
-              ncand += (r == kRows - 1 && b == 2) ? lstart[e + 1] - i - 1 : lstart[e + 1] - lstart[e];
-            }
+      const bool valid = k < T && (!(bpn >> 16) || jb > ia);
+      const int i = (bpa & 0xffff) + ia;
+      const int m = jb < (bp1 >> 16) ? (bp1 & 0xffff) + jb : bl2 + jb;
+      const float4 pi = pf[valid ? i : 0], pj = pf[valid ? m : 0];
+      float4 dq;  // positions are in the tile frame: no row offset
+      dq.x = pj.x - pi.x;
+      dq.y = pj.y - pi.y;
+      dq.z = pj.z - pi.z;
+      dq.w = fmaf(dq.x, dq.x, fmaf(dq.y, dq.y, dq.z * dq.z));
+      const int ti = __float_as_int(pi.w), tj = __float_as_int(pj.w);
+      if (COUNT && valid) {
+        ++ncand;
+        ++neval;
+      }
+      enqueue(valid && dq.w <= rcpre, dq, i | (m << 14) | (ti << 28) | (tj << 30));
+    }
+    __syncwarp();
+  };
+
+  int* ucnt = (int*)(red + 8 * nw);  // work-unit counter
+  if constexpr (!FP64) {
+    // ---- item building: (staged atom, owned row) pairs, laid end to end ----
+    // A unit is 32 consecutive staged atoms and one of kParts shares of each
+    // atom's list of owned rows (the rows whose ownership mask for the atom's
+    // position class is nonzero; ordinals n = kParts m + part).  The warp lays
+    // the unit's (atom, row) pairs end to end and builds one item per lane per
+    // step, so lanes do not idle on atoms that own few rows (the halo).  Units are handed out by a
+    // shared counter: their cost varies, and the force sums do not depend on the
+    // order.  An item is the atom's j-range(s) in the row: the owned cells,
+    // trimmed to those whose box comes within rc of the atom (the 1e-4 margin in
+    // prune2 covers the FP32 rounding; the accepted pairs are unchanged).
+    const int nunits = kParts * ((total + 31) >> 5);
+    const float prune2 = A.lj.prune2;
+    while (true) {
+      int u = 0;
+      if (lane == 0) u = atomicAdd(ucnt, 1);
+      u = __shfl_sync(FULL, u, 0);
+      if (u >= nunits) break;
+      const int c = u / kParts, part = u - c * kParts;
+      // per-atom quantities of lane l's atom c*32 + l
+      const int ia = c * 32 + lane;
+      const bool va = ia < total;
+      const int cia = code[va ? ia : 0];
+      const int ax = cia & 31, ay = (cia >> 5) & 31, az = cia >> 10;
+      const int acls = pos_class(ax - 1, tx) * 25 + pos_class(ay - 1, ty) * 5 + pos_class(az - 1, tz);
+      const int aw = va ? (sown->nrow[acls] + kParts - 1 - part) / kParts : 0;
+      const float4 pa = pf[va ? ia : 0];
+      const float apy = FP64 ? pa.y : oy[ay] + pa.y;  // tile-frame y, z
+      const float apz = FP64 ? pa.z : oz[az] + pa.z;
+      // squared x-gaps to the cells dx = -2, -1, +1, +2 (ox has EX + 1 entries)
+      const float gm2 = fmaxf(pa.x - ox[max(ax - 1, 0)], 0.f), gm1 = fmaxf(pa.x - ox[ax], 0.f);
+      const float gp1 = fmaxf(ox[min(ax + 1, EX)] - pa.x, 0.f), gp2 = fmaxf(ox[min(ax + 2, EX)] - pa.x, 0.f);
+      const float am2 = gm2 * gm2, am1 = gm1 * gm1, ap1 = gp1 * gp1, ap2 = gp2 * gp2;
+      int incl = aw;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int as0 = incl - aw, W = __shfl_sync(FULL, incl, 31);
+      const unsigned wb = __ballot_sync(FULL, aw > 0);
+      if (aw > 0) r2l[__popc(wb & lt)] = (unsigned char)lane;
+      __syncwarp();
+      int qb = 0;  // working atoms that start before K
+      for (int K = 0; K < W; K += 32) {
+        const unsigned M = __reduce_or_sync(FULL, (aw > 0 && (unsigned)(as0 - K) < 32u) ? 1u << (as0 - K) : 0u);
+        const int qr = qb + __popc(M & (FULL >> (31 - lane))) - 1;  // >= 0: the first worker starts at 0
+        qb += __popc(M);
+        const int k = K + lane;
+        const bool valid = k < W;
+        const int ql = r2l[qr];
+        const int s_q = __shfl_sync(FULL, as0, ql);
+        const int ci = __shfl_sync(FULL, cia, ql);
+        const int cls = __shfl_sync(FULL, acls, ql);
+        const float py = __shfl_sync(FULL, apy, ql), pz = __shfl_sync(FULL, apz, ql);
+        const float xm2 = __shfl_sync(FULL, am2, ql), xm1 = __shfl_sync(FULL, am1, ql);
+        const float xp1 = __shfl_sync(FULL, ap1, ql), xp2 = __shfl_sync(FULL, ap2, ql);
+        const int i = c * 32 + ql;
+        const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
+        int r = 0, mask = 0;
+        if (valid) {
+          r = sown->rlist[cls][kParts * (k - s_q) + part];
+          mask = sown->lut[cls][r];
         }
-        // distance from the atom to the row's cell boxes
-        const float gy = dy > 0 ? oy[ly + dy] - py : (dy < 0 ? py - oy[ly + dy + 1] : 0.f);
-        const float gz = dz > 0 ? oz[lz + dz] - pz : (dz < 0 ? pz - oz[lz + dz + 1] : 0.f);
-        const float g2 = fmaxf(gy, 0.f) * fmaxf(gy, 0.f) + fmaxf(gz, 0.f) * fmaxf(gz, 0.f);
-        const float tr = prune2 - g2;
-        if (tr < 0.f) mask = 0;
-        mask &= ~((xm2 > tr ? 1 : 0) | (xm1 > tr ? 2 : 0) | (xp1 > tr ? 8 : 0) | (xp2 > tr ? 16 : 0));
+        int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
         if (mask) {
+          const int dy = srows[2 * r], dz = srows[2 * r + 1];
+          const int rowbase = ((ly + dy) + EY * (lz + dz)) * EX + lx - 2;  // + bit b -> ext cell of dx = b - 2
+          if (COUNT) {  // every atom of the owned cells, as the reference visits them
+            for (int b = 0; b < 5; ++b)
+              if ((mask >> b) & 1) {
+                const int e = rowbase + b;
+                ncand += (r == kRows - 1 && b == 2) ? lstart[e + 1] - i - 1 : lstart[e + 1] - lstart[e];
+              }
+          }
+          // distance from the atom to the row's cell boxes
+          const float gy = dy > 0 ? oy[ly + dy] - py : (dy < 0 ? py - oy[ly + dy + 1] : 0.f);
+          const float gz = dz > 0 ? oz[lz + dz] - pz : (dz < 0 ? pz - oz[lz + dz + 1] : 0.f);
+          const float g2 = fmaxf(gy, 0.f) * fmaxf(gy, 0.f) + fmaxf(gz, 0.f) * fmaxf(gz, 0.f);
+          const float tr = prune2 - g2;
+          if (tr < 0.f) mask = 0;
+          mask &= ~((xm2 > tr ? 1 : 0) | (xm1 > tr ? 2 : 0) | (xp1 > tr ? 8 : 0) | (xp2 > tr ? 16 : 0));
+          if (mask) {
+            const int b0 = __ffs(mask) - 1, b1 = 31 - __clz(mask);
+            const int mm = mask >> b0;
+            lo1 = lstart[rowbase + b0];
+            int hi1 = lstart[rowbase + b1 + 1];
+            if (mm & (mm + 1)) {  // two runs: [b0, e1) and [b2, b1]
+              const int e1 = b0 + __ffs(~mm) - 1;
+              const int b2 = __ffs(mask & ~((1 << e1) - 1)) - 1;
+              lo2 = lstart[rowbase + b2];
+              n2 = hi1 - lo2;
+              hi1 = lstart[rowbase + e1];
+            }
+            n1 = hi1 - lo1;
+            if (r == kRows - 1 && b0 == 2) {  // pairs inside the cell: a2 > a1
+              n1 -= i + 1 - lo1;
+              lo1 = i + 1;
+            }
+            if (n1 <= 0) {
+              lo1 = lo2;
+              n1 = n2;
+              lo2 = 0;
+              n2 = 0;
+            }
+          }
+        }
+        consume(i, r, lo1, n1, lo2, n2);
+      }
+      __syncwarp();
+    }
+  } else {
+    // ---- item building: (ext cell, owned row) pairs, laid end to end ----
+    // A unit is 32 consecutive ext cells and one of kCellParts shares of each
+    // cell's owned rows; empty cells have no work.  An item is the row's owned
+    // j-cells as at most two contiguous runs (no per-atom trimming: the block
+    // is tested in full).
+    constexpr int kCellParts = 4;
+    const int nunits = kCellParts * ((NE + 31) >> 5);
+    while (true) {
+      int u = 0;
+      if (lane == 0) u = atomicAdd(ucnt, 1);
+      u = __shfl_sync(FULL, u, 0);
+      if (u >= nunits) break;
+      const int c = u / kCellParts, part = u - c * kCellParts;
+      const int e = c * 32 + lane;
+      const bool ve = e < NE;
+      const int ee = ve ? e : 0;
+      const int ex = ee % EX, er = ee / EX, ey = er % EY, ez = er / EY;
+      const int ai0 = lstart[ee], ana = ve ? lstart[ee + 1] - ai0 : 0;
+      const int acls = pos_class(ex - 1, tx) * 25 + pos_class(ey - 1, ty) * 5 + pos_class(ez - 1, tz);
+      const int aw = ana > 0 ? (sown->nrow[acls] + kCellParts - 1 - part) / kCellParts : 0;
+      int incl = aw;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int as0 = incl - aw, W = __shfl_sync(FULL, incl, 31);
+      const unsigned wb = __ballot_sync(FULL, aw > 0);
+      if (aw > 0) r2l[__popc(wb & lt)] = (unsigned char)lane;
+      __syncwarp();
+      const int ageo = ex | (ey << 5) | (ez << 10) | (acls << 15);
+      const int apa = ai0 | (ana << 16);
+      int qb = 0;
+      for (int K = 0; K < W; K += 32) {
+        const unsigned M = __reduce_or_sync(FULL, (aw > 0 && (unsigned)(as0 - K) < 32u) ? 1u << (as0 - K) : 0u);
+        const int qr = qb + __popc(M & le) - 1;
+        qb += __popc(M);
+        const int k = K + lane;
+        const bool valid = k < W;
+        const int ql = r2l[qr];
+        const int s_q = __shfl_sync(FULL, as0, ql);
+        const int geo = __shfl_sync(FULL, ageo, ql);
+        const int qpa = __shfl_sync(FULL, apa, ql);
+        const int lx = geo & 31, ly = (geo >> 5) & 31, lz = (geo >> 10) & 31, cls = geo >> 15;
+        int r = 0, mask = 0;
+        if (valid) {
+          r = sown->rlist[cls][kCellParts * (k - s_q) + part];
+          mask = sown->lut[cls][r];
+        }
+        int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
+        bool self = false;
+        if (mask) {
+          const int dy = srows[2 * r], dz = srows[2 * r + 1];
+          const int rowbase = ((ly + dy) + EY * (lz + dz)) * EX + lx - 2;  // + bit b -> ext cell of dx = b - 2
           const int b0 = __ffs(mask) - 1, b1 = 31 - __clz(mask);
           const int mm = mask >> b0;
           lo1 = lstart[rowbase + b0];
@@ -599,21 +757,18 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
             hi1 = lstart[rowbase + e1];
           }
           n1 = hi1 - lo1;
-          if (r == kRows - 1 && b0 == 2) {  // pairs inside the cell: a2 > a1
-            n1 -= i + 1 - lo1;
-            lo1 = i + 1;
-          }
-          if (n1 <= 0) {
+          self = r == kRows - 1 && b0 == 2;  // the first run starts at the cell itself
+          if (n1 <= 0 && !self) {
             lo1 = lo2;
             n1 = n2;
             lo2 = 0;
             n2 = 0;
           }
         }
+        consume_cells(qpa & 0xffff, qpa >> 16, lo1, n1, lo2, n2, self);
       }
-      consume(i, r, lo1, n1, lo2, n2);
+      __syncwarp();
     }
-    __syncwarp();
   }
   if (qn > 0) {  // the last, partial batch
     __syncwarp();
