@@ -214,10 +214,15 @@ def cpu_baseline(pos, L, reps=2):
     for _ in range(reps):
         O.forces_typed(pos, np.full(3, L), RC, threads=cores)
     t = (time.perf_counter() - t0) / reps
+    t1 = time.perf_counter()
+    O.forces_typed(pos, np.full(3, L), RC, threads=1)  # one core, as one reference MPI rank runs
+    t1 = time.perf_counter() - t1
     return {"value": len(pos) / t, "unit": "atom-steps/s", "cores": cores, "kind": "port",
             "sample": f"{reps} force evaluations of the {len(pos)}-atom workload by the C restatement of "
                       f"exaMD_forces_midpoint_all (OpenMP over home blocks, {cores} threads); "
-                      f"{t:.3f} s each; integration O(N) neglected"}
+                      f"{t:.3f} s each; integration O(N) neglected",
+            "single_core": {"value": len(pos) / t1, "cores": 1,
+                            "sample": f"1 force evaluation on one thread, {t1:.3f} s"}}
 
 
 def run_reference(args, ws, rk):
@@ -387,7 +392,12 @@ def main():
                        "parallelism": f"replicas{ws}"},
             "clocks": clk.summary(),
             "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n},
-            "gpu_launches": 7 * args.steps + 1,
+            # per step: kick+drift+bin, 3 scan kernels, place, finalize, pair, side-list apply
+            "gpu_launches": 8 * args.steps + 1,
+            # pair rates of the timed run (the counters of one force evaluation x steps / time)
+            "pairs": {"interactions_per_s": cnt["accepted"] * args.steps * ws / (t_ms * 1e-3),
+                      "candidates_per_s": cnt["candidates"] * args.steps * ws / (t_ms * 1e-3),
+                      "kernel_interactions_per_s": cnt["accepted"] / (k_ms * 1e-3)},
             "roofline": {"bound": "fp32", "kernel": "k_pair (mixed)", "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "traffic": traffic, "kernel_ms": k_ms, "flops_per_launch": flops,

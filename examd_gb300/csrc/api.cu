@@ -166,6 +166,8 @@ struct examd_ctx {
   double* tileE = nullptr;
   double* tileW = nullptr;
   long long* tileC = nullptr;
+  int* redo = nullptr;  // mixed form: tiles for the redo pass (large pair-force terms)
+  int* redo_n = nullptr;  // [0] count, [1] done counter of the redo pass
   double* boxE = nullptr;  // per box (graph chunk: [chunk][nboxes])
   double* boxW = nullptr;
   double* boxKE = nullptr;
@@ -229,7 +231,7 @@ void free_all(examd_ctx* ctx) {
                   ctx->cellOld, ctx->slot, ctx->src, ctx->count, ctx->cstart, ctx->bsum, ctx->d_total,
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
                   ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor,
-                  ctx->d_atom0, ctx->keAtom, ctx->partial};
+                  ctx->d_atom0, ctx->keAtom, ctx->partial, ctx->redo, ctx->redo_n};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (int b = 0; b < 2; ++b) {
@@ -605,6 +607,8 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     ctx->Fown = f;
     ALLOC(f, 7 * N);
     ctx->P = f;
+    ALLOC(ctx->redo, std::max(1, ctx->ntiles));
+    ALLOC(ctx->redo_n, 2);
   }
   ALLOC(ctx->tileE, ctx->ntiles);
   ALLOC(ctx->tileW, ctx->ntiles);
@@ -644,6 +648,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
                             cudaMemcpyHostToDevice, st) == cudaSuccess &&
             cudaMemsetAsync(ctx->count, 0, NC * sizeof(int), st) == cudaSuccess &&
             cudaMemsetAsync(ctx->status, 0, sizeof(int), st) == cudaSuccess &&
+            (!ctx->redo_n || cudaMemsetAsync(ctx->redo_n, 0, 2 * sizeof(int), st) == cudaSuccess) &&
             cudaStreamSynchronize(st) == cudaSuccess;
   if (!ok) {
     free_all(ctx);
@@ -782,6 +787,9 @@ PairArgs pair_args(examd_ctx* ctx) {
   a.cap = ctx->cap;
   a.ne_max = ctx->ne_max;
   a.lj = ctx->lj;
+  a.redo = ctx->redo;
+  a.redo_n = ctx->redo_n;
+  a.redo_done = (unsigned*)(ctx->redo_n + 1);
   return a;
 }
 

@@ -46,6 +46,11 @@ struct PairArgs {
   int cap;     // staged-atom capacity of a tile
   int ne_max;  // largest ext-cell count of a tile
   LJTable lj;
+  // mixed form: tiles whose pair-force terms exceeded the fixed-point range,
+  // for the redo pass (ntiles entries; count and done counter zero between launches)
+  int* redo;
+  int* redo_n;
+  unsigned* redo_done;
 };
 
 struct PairConfig {
@@ -57,6 +62,8 @@ struct PairConfig {
   int warps = 8;
 };
 
+// Dynamic shared memory for a tile capacity: the larger of the two passes'
+// needs (the mixed form's redo pass may need more).
 int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max);
 cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes);  // opt-in smem attribute
 cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st);

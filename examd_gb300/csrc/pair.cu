@@ -28,16 +28,21 @@
 // Accumulation.  Mixed form: each per-atom force component is an exact 32-bit
 // fixed-point sum in shared memory (scale 2^15, native integer atomics), so
 // the result does not depend on the order of the terms and is reproducible
-// bit for bit.  A term of magnitude >= 1024 (r < 0.79 sigma at eps = 1)
-// takes an FP32 side path instead, so every fixed-point term is below 2^25
-// and a component's sum could leave the int32 range only through more than
-// 64 near-maximal terms of one sign on one atom, i.e. 64 neighbours within
-// about 0.8 sigma on one side, which no physical configuration has.  FP64
-// form: FP64 shared-memory atomics.  No global atomics are used.
+// bit for bit.  A term of magnitude >= 1024 (r < 0.79 sigma at eps = 1) is
+// left out and flags the tile, so every fixed-point term is below 2^25 and a
+// component's sum could leave the int32 range only through more than 64
+// near-maximal terms of one sign on one atom, i.e. 64 neighbours within about
+// 0.8 sigma on one side, which no physical configuration has.  A second
+// launch (k_pair_redo) recomputes the flagged tiles, sums their large terms
+// in FP32 and adds them to the outputs; thermal configurations flag no tile
+// and the launch returns at once (only the rare FP32 sums' order can vary
+// between runs).  FP64 form: FP64 shared-memory atomics.
 //
 // Output: forces of the tile's home atoms go to Fown, those of halo copies to
 // the partial slot P[s] (s = bitmask of the axes on which the copy is a halo
 // copy); the integrator sums an atom's 1..8 partials in a fixed order.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "pairfn.cuh"
@@ -53,18 +58,28 @@ constexpr int kQueue = 64;    // per-warp queue of accepted pairs
 constexpr int kParts = 2;     // work units per 32 staged atoms (1, 3 and 4 measured slower)
 constexpr float kFix = 32768.f;        // fixed-point scale 2^15
 constexpr float kFixInv = 1.f / 32768.f;
-constexpr float kFixMax = 1024.f;      // larger terms take the FP32 side path
+constexpr float kFixMax = 1024.f;      // larger terms are left to the redo pass
+constexpr int kRedoBlocks = 304;       // grid of the redo pass (2 per SM)
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
   int lstart, gfirst, ox, oy, oz, dyt, dzt, img, red, r2l, lut, queue;
-  int pf, fa, fr, px, code;
+  int pf, fa, px, code, fr;
   int bytes;
 };
 
+// Per-warp tables after the accepted-pair queues.  Mixed form: one step's
+// items by rank (float4 ptA + int4 ptB each) and the work unit's atoms by
+// rank (2 float4 each).  FP64 form: one step's items by lane (float4).
+constexpr int kWarpTabMixed = 32 * 16 + 32 * 16 + 32 * 32;
+constexpr int kWarpTabFp64 = 32 * 16;
+
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
-__host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int nw) {
+// redo: the mixed form's pass over tiles with large terms (fr: their FP32
+// sums, over the accepted-pair queues, which that pass does not use, when
+// they fit there).
+__host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int nw, bool redo = false) {
   Layout L;
   int o = 0;
   L.lstart = o; o = align16(o + 4 * (ne_max + 1));
@@ -75,27 +90,31 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.dyt = o;    o = align16(o + 4 * kMaxExt * kDT);
   L.dzt = o;    o = align16(o + 4 * kMaxExt * kDT);
   L.img = o;    o = align16(o + (fp64 ? 3 * 32 : 0));  // periodic image per ext coordinate (FP64 form)
-  L.red = o;    o = align16(o + 8 * 8 * nw + 16);  // + the CTA's unit counter
-  L.r2l = o;    o = align16(o + 64 * nw);
+  L.red = o;    o = align16(o + 8 * 8 * nw + 16);  // + the unit counter and the large-term flag
+  L.r2l = o;    o = align16(o + (fp64 ? 64 * nw : 0));  // rank -> lane tables (FP64 form)
   L.lut = o;    o = align16(o + (int)sizeof(OwnLut));
-  L.queue = o;  o = align16(o + ((fp64 ? 4 : 20) * kQueue + 16 * 32) * nw);  // + one step's item table
+  const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64 : 20 * kQueue + kWarpTabMixed) * nw;
+  L.queue = o;  o = align16(o + qbytes);
   L.pf = o;     o = align16(o + 16 * cap);
   if (fp64) {
     L.fa = o;   o = align16(o + 3 * 8 * cap);  // FP64 force sums
-    L.fr = o;
     L.px = o;   o = align16(o + 3 * 8 * cap);  // FP64 positions
   } else {
     L.fa = o;   o = align16(o + 3 * 4 * cap);  // fixed-point force sums
-    L.fr = o;   o = align16(o + 3 * 4 * cap);  // FP32 side path for large terms
     L.px = o;
   }
   L.code = o;   o = align16(o + 2 * cap);
+  L.fr = L.queue;
+  if (redo && !fp64 && 3 * 4 * cap > 20 * kQueue * nw) {
+    L.fr = o;   o = align16(o + 3 * 4 * cap);
+  }
   L.bytes = o;
   return L;
 }
 
 int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max) {
-  return make_layout(cfg.fp64, cap, ne_max, cfg.warps).bytes;
+  const int main = make_layout(cfg.fp64, cap, ne_max, cfg.warps).bytes;
+  return cfg.fp64 ? main : std::max(main, make_layout(false, cap, ne_max, cfg.warps, true).bytes);
 }
 
 // Exact sum of FP32 terms in 64-bit fixed point (2^-32 resolution): the total
@@ -124,10 +143,16 @@ struct FixSum {
 // (a segmented shuffle scan; integer sums, so the result is exact) and the
 // run's last lane adds the total: one shared atomic per run instead of one
 // per pair on the same address.
+// A pair-force term too large for the fixed-point sums (a component of
+// magnitude >= kFixMax, i.e. r < ~0.79 sigma at eps = 1, which thermal
+// configurations do not reach) is left out here and raises the tile's flag
+// (*big_flag); the redo pass adds it.
 template <bool MULTI, bool ENERGY, bool COUNT>
-__device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, const int* qk, int* fa, float* fr,
-                                            int cap, const LJTable& lj, FixSum& ek, FixSum& wk, int* status,
-                                            int& nacc) {
+__device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, const int* qk, int* fa,
+                                            const PairArgs& A, FixSum& ek, FixSum& wk, int& nacc,
+                                            int* big_flag) {
+  const int cap = A.cap;
+  const LJTable& lj = A.lj;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const bool act = lane < cnt;
@@ -154,10 +179,10 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, c
       }
       if (COUNT) ++nacc;
     } else if (rv < 0) {
-      atomicOr(status, ST_PAIRFN);
+      atomicOr(A.status, ST_PAIRFN);
     }
   }
-  // terms too large for the fixed-point sums take the FP32 side path
+  // terms too large for the fixed-point sums: left to the redo pass
   const bool big = act && fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) >= kFixMax * kFix;
   int ix = 0, iy = 0, iz = 0;
   if (act && !big) {
@@ -168,14 +193,7 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, c
     atomicAdd(&fa[cap + m], -iy);
     atomicAdd(&fa[2 * cap + m], -iz);
   }
-  if (big) {
-    atomicAdd(&fr[i], fx * kFixInv);
-    atomicAdd(&fr[cap + i], fy * kFixInv);
-    atomicAdd(&fr[2 * cap + i], fz * kFixInv);
-    atomicAdd(&fr[m], -fx * kFixInv);
-    atomicAdd(&fr[cap + m], -fy * kFixInv);
-    atomicAdd(&fr[2 * cap + m], -fz * kFixInv);
-  }
+  if (big) *big_flag = 1;
   // i side: sum over runs of equal i (inactive lanes form one run with i = -1),
   // in segments of 8 lanes from the run's first one: each segment's last lane
   // adds the segment's total
@@ -247,19 +265,22 @@ __device__ __forceinline__ void force_batch64(int cnt, const int* qk, const doub
   }
 }
 
-template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
-__global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
+// One tile.  REDO (mixed form only, without energy or counters): the pass
+// over the tiles whose first pass met a large term; it recomputes the tile's
+// pairs, sums only the large terms (FP32 shared atomics) and adds them to the
+// outputs that the first pass wrote.
+template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, bool REDO>
+__device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  const int tile = blockIdx.x;
   const int4 t0 = A.tiles[2 * tile], t1 = A.tiles[2 * tile + 1];
   const BoxDev& B = A.boxes[t0.x];
   const int X0 = t0.y, Y0 = t0.z, Z0 = t0.w;
   const int tx = t1.x, ty = t1.y, tz = t1.z;
   const int EX = tx + 2, EY = ty + 2, EZ = tz + 2;
   const int NE = EX * EY * EZ;
-  const Layout L = make_layout(FP64, A.cap, A.ne_max, nw);
+  const Layout L = make_layout(FP64, A.cap, A.ne_max, nw, REDO);
   int* lstart = (int*)(smem + L.lstart);
   int* gfirst = (int*)(smem + L.gfirst);
   float* ox = (float*)(smem + L.ox);
@@ -377,7 +398,7 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   }
   // (3) stage atoms, one thread per ext cell
   int* fa = (int*)(smem + L.fa);
-  float* fr = (float*)(smem + L.fr);
+  float* fr = (float*)(smem + L.fr);  // redo pass: FP32 sums of the large terms
   double* fd = (double*)(smem + L.fa);
   double* pd = (double*)(smem + L.px);
   for (int e = tid; e < NE; e += blockDim.x) {
@@ -398,14 +419,21 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
         pf[t] = make_float4(ox[lx] + u.x, u.y, u.z, u.w);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          fa[c * cap + t] = 0;
-          fr[c * cap + t] = 0.f;
+          if (REDO)
+            fr[c * cap + t] = 0.f;
+          else
+            fa[c * cap + t] = 0;
         }
       }
       code[t] = cc;
     }
   }
-  if (tid == 0) *(int*)(red + 8 * nw) = 0;  // work-unit counter
+  int* cw = (int*)(red + 8 * nw);
+  int* big_flag = cw + 1;  // mixed form: a term was too large for the fixed-point sums
+  if (tid == 0) {
+    cw[0] = 0;  // work-unit counter
+    *big_flag = 0;
+  }
   __syncthreads();
 
   const LJ32 q32 = A.lj.p32[0];
@@ -418,13 +446,16 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   constexpr int kQd = FP64 ? 0 : 16;
   float4* qd = (float4*)(smem + L.queue) + warp * kQueue;
   int* qk = (int*)(smem + L.queue + kQd * kQueue * nw) + warp * kQueue;
-  // per-warp table of one step's items: (C, key base)
-  float4* ptA = (float4*)(smem + L.queue + (kQd + 4) * kQueue * nw) + warp * 32;
+  // per-warp tables (kWarpTab*): one step's items (ptA, ptB) and, mixed
+  // form, the work unit's atoms (bt)
+  unsigned char* wtab = smem + L.queue + (kQd + 4) * kQueue * nw + warp * (FP64 ? kWarpTabFp64 : kWarpTabMixed);
+  float4* ptA = (float4*)wtab;
+  int4* ptB = (int4*)(wtab + 32 * 16);
+  float4* bt = (float4*)(wtab + 32 * 32);
   int qn = 0, qh = 0;  // queued pairs and the ring's head
   const unsigned lt = (1u << lane) - 1u;
   const unsigned le = FULL >> (31 - lane);
-  unsigned char* r2l = smem + L.r2l + 64 * warp;  // two rank -> lane tables of 32
-
+  unsigned char* r2l = smem + L.r2l + 64 * warp;  // FP64 form: two rank -> lane tables of 32
   // ---- accepted pairs go to the warp's queue (a ring of kQueue entries);
   // their forces are computed in full batches of 32 ----
   auto enqueue = [&](bool acc, const float4& dq, int key) {
@@ -441,18 +472,39 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
         force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
                                             qh);
       else
-        force_batch<MULTI, ENERGY, COUNT>(32, qh, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
+        force_batch<MULTI, ENERGY, COUNT>(32, qh, qd, qk, fa, A, ek, wk, nacc, big_flag);
       __syncwarp();
       qh = (qh + 32) & (kQueue - 1);
       qn -= 32;
     }
   };
 
+  // ---- redo pass: the force of each accepted pair at once; only the large
+  // terms, decided exactly as force_batch decides them, are summed (both atoms)
+  auto redo_pair = [&](bool acc, const float4& dq, int key) {
+    if (!acc) return;
+    const int i = key & 0x3fff, m = (key >> 14) & 0x3fff;
+    LJ32 P = A.lj.p32[0];
+    if (MULTI) P = A.lj.p32[((key >> 28) & 3) * A.lj.nt + ((unsigned)key >> 30)];
+    float dg = 0.f, e = 0.f;
+    if (pair_fn32<false>(A.lj.pot, dq.w, P, dg, e) != 0) return;
+    const float dgs = kFix * dg;
+    const float fx = dgs * dq.x, fy = dgs * dq.y, fz = dgs * dq.z;
+    if (!(fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) >= kFixMax * kFix)) return;
+    atomicAdd(&fr[i], fx * kFixInv);
+    atomicAdd(&fr[cap + i], fy * kFixInv);
+    atomicAdd(&fr[2 * cap + i], fz * kFixInv);
+    atomicAdd(&fr[m], -fx * kFixInv);
+    atomicAdd(&fr[cap + m], -fy * kFixInv);
+    atomicAdd(&fr[2 * cap + m], -fz * kFixInv);
+  };
+
   // ---- mixed form: consume one step's (atom, row) items, at most one per
   // lane (nt = 0: none).  The items' candidate pairs are laid end to end and
   // the warp walks them 32 at a time, one pair per lane, so no lane idles
   // while another finishes a long j-range.  A lane finds its item from the
-  // bitmask of the items that start in the current 32 candidates.
+  // bitmask of the items that start in the current 32 candidates, and reads
+  // the item's data from the per-warp tables by its rank.
   auto consume = [&](int i, int r, int lo1, int n1, int lo2, int n2) {
     const int nt = n1 + n2;
     const unsigned hb = __ballot_sync(FULL, nt > 0);
@@ -466,7 +518,6 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
     }
     const int s0 = incl - nt;
     const int T = __shfl_sync(FULL, incl, 31);
-    const int p1 = lo1 | (n1 << 16), l2 = lo2 - n1;
     if (nt > 0) {
       // the atom's position moved into the j-cells' frame: d = x_j + C
       // (y, z relative to the cell origin)
@@ -476,8 +527,11 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
       const int dy = srows[2 * r], dz = srows[2 * r + 1];
       const float Cy = dyt[ly * kDT + dy + 2] - pi.y;
       const float Cz = dzt[lz * kDT + dz + 2] - pi.z;
-      ptA[lane] = make_float4(-pi.x, Cy, Cz, __int_as_float(i | (__float_as_int(pi.w) << 28)));
-      r2l[32 + __popc(hb & lt)] = (unsigned char)lane;
+      // by rank: the item's key base and frame shift, and the offsets that map
+      // candidate k to its staged atom: m = k + (k < e1 ? o1 : o2)
+      const int rk = __popc(hb & lt);
+      ptA[rk] = make_float4(-pi.x, Cy, Cz, __int_as_float(i | (__float_as_int(pi.w) << 28)));
+      ptB[rk] = make_int4(lo1 - s0, s0 + n1, lo2 - n1 - s0, 0);
     }
     __syncwarp();
     // distance tests; accepted pairs go to the queue
@@ -486,13 +540,11 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
       const unsigned M = __reduce_or_sync(FULL, (nt > 0 && (unsigned)(s0 - K) < 32u) ? 1u << (s0 - K) : 0u);
       const int qr = qb + __popc(M & le) - 1;  // >= 0: the first item starts at 0
       qb += __popc(M);
-      const int ql = r2l[32 + qr];
-      const int bp1 = __shfl_sync(FULL, p1, ql), bl2 = __shfl_sync(FULL, l2, ql), bs = __shfl_sync(FULL, s0, ql);
-      const float4 a = ptA[ql];
+      const float4 a = ptA[qr];
+      const int4 b = ptB[qr];
       const int k = K + lane;
       const bool valid = k < T;
-      const int mo = k - bs;
-      const int m = mo < (bp1 >> 16) ? (bp1 & 0xffff) + mo : bl2 + mo;
+      const int m = (k < b.y ? b.x : b.z) + k;
       const float4 pj = pf[valid ? m : 0];
       float4 dq;
       dq.x = pj.x + a.x;
@@ -503,7 +555,10 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
       const int kb = __float_as_int(a.w);
       if (COUNT && valid) ++neval;
       const float thr = MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
-      enqueue(valid && dq.w <= thr, dq, kb | (m << 14) | (tj << 30));
+      if (REDO)
+        redo_pair(valid && dq.w <= thr, dq, kb | (m << 14) | (tj << 30));
+      else
+        enqueue(valid && dq.w <= thr, dq, kb | (m << 14) | (tj << 30));
     }
     __syncwarp();
   };
@@ -578,7 +633,7 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
     __syncwarp();
   };
 
-  int* ucnt = (int*)(red + 8 * nw);  // work-unit counter
+  int* ucnt = cw;  // work-unit counter
   if constexpr (!FP64) {
     // ---- item building: (staged atom, owned row) pairs, laid end to end ----
     // A unit is 32 consecutive staged atoms and one of kParts shares of each
@@ -620,7 +675,11 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
       }
       const int as0 = incl - aw, W = __shfl_sync(FULL, incl, 31);
       const unsigned wb = __ballot_sync(FULL, aw > 0);
-      if (aw > 0) r2l[__popc(wb & lt)] = (unsigned char)lane;
+      if (aw > 0) {  // the working atoms' data by rank (as0 < 512, ia < 2^14, acls < 128)
+        const int rk = __popc(wb & lt);
+        bt[rk] = make_float4(apy, apz, am2, am1);
+        bt[32 + rk] = make_float4(ap1, ap2, __int_as_float(as0 | (ia << 9)), __int_as_float(cia | (acls << 15)));
+      }
       __syncwarp();
       int qb = 0;  // working atoms that start before K
       for (int K = 0; K < W; K += 32) {
@@ -629,14 +688,11 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
         qb += __popc(M);
         const int k = K + lane;
         const bool valid = k < W;
-        const int ql = r2l[qr];
-        const int s_q = __shfl_sync(FULL, as0, ql);
-        const int ci = __shfl_sync(FULL, cia, ql);
-        const int cls = __shfl_sync(FULL, acls, ql);
-        const float py = __shfl_sync(FULL, apy, ql), pz = __shfl_sync(FULL, apz, ql);
-        const float xm2 = __shfl_sync(FULL, am2, ql), xm1 = __shfl_sync(FULL, am1, ql);
-        const float xp1 = __shfl_sync(FULL, ap1, ql), xp2 = __shfl_sync(FULL, ap2, ql);
-        const int i = c * 32 + ql;
+        const float4 b0v = bt[qr], b1v = bt[32 + qr];
+        const float py = b0v.x, pz = b0v.y, xm2 = b0v.z, xm1 = b0v.w, xp1 = b1v.x, xp2 = b1v.y;
+        const int sq = __float_as_int(b1v.z), cc = __float_as_int(b1v.w);
+        const int s_q = sq & 511, i = sq >> 9;
+        const int ci = cc & 0x7fff, cls = cc >> 15;
         const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
         int r = 0, mask = 0;
         if (valid) {
@@ -776,9 +832,11 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
       force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
                                           qh);
     else
-      force_batch<MULTI, ENERGY, COUNT>(qn, qh, qd, qk, fa, fr, cap, A.lj, ek, wk, A.status, nacc);
+      force_batch<MULTI, ENERGY, COUNT>(qn, qh, qd, qk, fa, A, ek, wk, nacc, big_flag);
   }
   __syncthreads();
+  // a large term was left out: list the tile for the redo pass
+  if (!FP64 && !REDO && tid == 0 && *big_flag) A.redo[atomicAdd(A.redo_n, 1)] = tile;
 
   // (4) write-back: home atoms -> Fown, halo copies -> P[slot]
   for (int t = tid; t < total; t += blockDim.x) {
@@ -793,11 +851,24 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) F[c * A.N + g] = fd[c * cap + t];
     } else {
-      float f[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) f[c] = fmaf((float)fa[c * cap + t], kFixInv, fr[c * cap + t]);
       float4* F = slot == 0 ? (float4*)A.Fown : (float4*)A.P + (size_t)(slot - 1) * A.N;
-      F[g] = make_float4(f[0], f[1], f[2], 0.f);
+      if (REDO) {
+        // this copy's output was written by the first pass and by this tile
+        // only (a copy's slot pattern is unique to one tile)
+        const float x = fr[t], y = fr[cap + t], z = fr[2 * cap + t];
+        if (x != 0.f || y != 0.f || z != 0.f) {
+          float4 v = F[g];
+          v.x += x;
+          v.y += y;
+          v.z += z;
+          F[g] = v;
+        }
+      } else {
+        float f[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f[c] = (float)fa[c * cap + t] * kFixInv;
+        F[g] = make_float4(f[0], f[1], f[2], 0.f);
+      }
     }
   }
 
@@ -862,6 +933,31 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
 }
 
 template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
+__global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
+  pair_tile<FP64, MULTI, ENERGY, COUNT, false>(A, blockIdx.x);
+}
+
+// Mixed form: the redo pass over the tiles that k_pair listed (normally none,
+// and the blocks return at once).  The block that finishes last empties the
+// list; every block has read its length before any block counts itself done.
+template <bool MULTI>
+__global__ void __launch_bounds__(256, 3) k_pair_redo(const PairArgs A) {
+  const int n = *(volatile const int*)A.redo_n;
+  for (int j = blockIdx.x; j < n; j += gridDim.x) {
+    pair_tile<false, MULTI, false, false, true>(A, A.redo[j]);
+    __syncthreads();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(A.redo_done, 1u) == gridDim.x - 1) {
+      *A.redo_n = 0;
+      *A.redo_done = 0;
+    }
+  }
+}
+
+template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
 static void* kfn() {
   return (void*)&k_pair<FP64, MULTI, ENERGY, COUNT>;
 }
@@ -881,15 +977,30 @@ static void* pick(const PairConfig& c) {
 #undef EXAMD_PICK
 }
 
+static void* pick_redo(const PairConfig& c) {
+  return c.multi ? (void*)&k_pair_redo<true> : (void*)&k_pair_redo<false>;
+}
+
 cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes) {
-  return cudaFuncSetAttribute(pick(cfg), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  cudaError_t e = cudaFuncSetAttribute(pick(cfg), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  if (e != cudaSuccess || cfg.fp64) return e;
+  return cudaFuncSetAttribute(pick_redo(cfg), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
 }
 
 cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st) {
   if (ntiles <= 0) return cudaSuccess;
   void* fn = pick(cfg);
   void* args[] = {(void*)&a};
-  return cudaLaunchKernel(fn, dim3(ntiles), dim3(32 * cfg.warps), args, (size_t)smem_bytes, st);
+  // smem_bytes (the larger of the two passes' needs) bounds both launches
+  const int main_smem = make_layout(cfg.fp64, a.cap, a.ne_max, cfg.warps).bytes;
+  if (main_smem > smem_bytes) return cudaErrorInvalidValue;
+  cudaError_t e = cudaLaunchKernel(fn, dim3(ntiles), dim3(32 * cfg.warps), args, (size_t)main_smem, st);
+  if (e != cudaSuccess || cfg.fp64) return e;
+  // the redo pass: a few blocks per SM at most; nothing to do in a thermal system
+  const int redo_smem = make_layout(false, a.cap, a.ne_max, cfg.warps, true).bytes;
+  if (redo_smem > smem_bytes) return cudaErrorInvalidValue;
+  return cudaLaunchKernel(pick_redo(cfg), dim3(std::min(ntiles, kRedoBlocks)), dim3(32 * cfg.warps), args,
+                          (size_t)redo_smem, st);
 }
 
 }  // namespace examd

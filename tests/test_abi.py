@@ -36,6 +36,19 @@ def test_strerror_and_defaults(gpulib):
     assert p.ntypes == 1 and p.rc[0] == 2.5 and p.eps[0] == 1.0 and p.precision == _lib.FP64
 
 
+def test_error_codes_match_header(gpulib):
+    """Every EXAMD_ERR_* of the header has the same value in the Python layer
+    and a message of its own."""
+    from examd_gb300 import _lib
+    L = _lib.load()
+    src = open(os.path.join(ROOT, "include", "examd_gb300.h")).read()
+    codes = dict(re.findall(r"#define EXAMD_(ERR_\w+)\s+(\d+)", src))
+    assert len(codes) >= 12
+    for name, val in codes.items():
+        assert getattr(_lib, name) == int(val), name
+        assert L.examd_gpu_strerror(int(val)) != b"unknown status", name
+
+
 def test_host_generators(gpulib):
     pos, L = gpulib.gen_fcc(3, 0.8442)
     assert pos.shape == (108, 3) and abs(L - 3 * (4 / 0.8442) ** (1 / 3)) < 1e-12
