@@ -48,6 +48,7 @@ class Params(C.Structure):
         ("strict_box", C.c_int),
         ("device", C.c_int),
         ("potential", C.c_int),
+        ("pair_tables", C.c_int),
     ]
 
 

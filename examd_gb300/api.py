@@ -43,10 +43,11 @@ def _table(v, nt):
 
 
 POTENTIALS = {"lj": _L.POT_LJ, "lj_shifted": _L.POT_LJ_SHIFTED, "wca": _L.POT_WCA}
+PAIR_TABLES = {"auto": 0, "wide": 1, "compact": 2}
 
 
 def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None, block_length=None,
-           tile=None, warps=None, strict_box=False, device=0, potential="lj"):
+           tile=None, warps=None, strict_box=False, device=0, potential="lj", pair_tables="auto"):
     """examd_params and the examd_box array of a system, from Python arguments."""
     lib = _L.load()
     b = np.atleast_2d(np.asarray(boxes, dtype=np.float64))
@@ -77,6 +78,9 @@ def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, 
     if potential not in POTENTIALS:
         raise ValueError(f"potential must be one of {sorted(POTENTIALS)}")
     p.potential = POTENTIALS[potential]
+    if pair_tables not in PAIR_TABLES:
+        raise ValueError(f"pair_tables must be one of {sorted(PAIR_TABLES)}")
+    p.pair_tables = PAIR_TABLES[pair_tables]
     arr = (_L.Box * b.shape[0])()
     for k in range(b.shape[0]):
         for a in range(3):
@@ -108,12 +112,15 @@ class MidpointLJ:
     positions, integration and reductions).  eps/sigma/rc: scalars or
     (ntypes, ntypes) tables; block_length defaults to max(rc)/2 as the
     reference (exaMD.f90:56).  potential: the pair function, "lj" (the
-    reference's lennardjones_12), "lj_shifted" or "wca"."""
+    reference's lennardjones_12), "lj_shifted" or "wca".  pair_tables: the
+    mixed form's per-warp tables, "auto" (compact where that fits more CTAs
+    on an SM), "wide" or "compact"; the forces are the same bit for bit."""
 
     def __init__(self, boxes, natoms, *, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None,
-                 block_length=None, tile=None, warps=None, strict_box=False, device=0, potential="lj"):
+                 block_length=None, tile=None, warps=None, strict_box=False, device=0, potential="lj",
+                 pair_tables="auto"):
         lib, p, arr, b, n, m = _setup(boxes, natoms, precision, eps, sigma, rc, ntypes, mass, block_length, tile,
-                                      warps, strict_box, device, potential)
+                                      warps, strict_box, device, potential, pair_tables)
         self._lib = lib
         self.nboxes = int(b.shape[0])
         self.natoms = n.copy()

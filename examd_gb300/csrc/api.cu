@@ -136,6 +136,7 @@ struct examd_ctx {
   LJTable lj{};
   PairConfig pc;
   int cap = 0, smem = 0, smem_limit = 0;
+  int pair_tables = 0;  // examd_params.pair_tables
   int dev = 0;
   cudaStream_t st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
@@ -386,7 +387,12 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   // pair-kernel configuration
   ctx->pc.fp64 = p.precision == EXAMD_FP64;
   ctx->pc.multi = nt > 1;
-  ctx->pc.kahan = true;
+  ctx->pc.pack = p.pair_tables == 2;
+  ctx->pair_tables = p.pair_tables;
+  if (p.pair_tables < 0 || p.pair_tables > 2) {
+    delete ctx;
+    return EXAMD_ERR_ARG;
+  }
   ctx->pc.warps = p.warps > 0 ? p.warps : 8;
   if (ctx->pc.warps < 4 || ctx->pc.warps > 8) {
     delete ctx;
@@ -748,13 +754,32 @@ int update_capacity(examd_ctx* ctx) {
   CK(cudaStreamSynchronize(ctx->st));
   int want = ((occ + occ / 4 + 64) + 31) & ~31;
   if (want <= ctx->cap) return EXAMD_OK;
-  int bytes = pair_smem_bytes(ctx->pc, want, ctx->ne_max);
+  // mixed form with pair_tables = 0: the compact per-warp tables where they
+  // fit more CTAs on an SM at this capacity (or where only they fit at all)
+  auto choose = [&](int cap) {
+    PairConfig c = ctx->pc;
+    if (c.fp64 || ctx->pair_tables != 0) return c;
+    PairConfig w = c, k = c;
+    w.pack = false;
+    k.pack = true;
+    for (int e = 0; e < 2; ++e) {  // the occupancy query needs the opt-in limit set
+      PairConfig q = e ? k : w;
+      if (pair_prepare(q, ctx->smem_limit) != cudaSuccess) return c;
+    }
+    c.pack = pair_smem_bytes(w, cap, ctx->ne_max) > ctx->smem_limit ||
+             pair_blocks_per_sm(k, cap, ctx->ne_max) > pair_blocks_per_sm(w, cap, ctx->ne_max);
+    return c;
+  };
+  PairConfig pc = choose(want);
+  int bytes = pair_smem_bytes(pc, want, ctx->ne_max);
   if (bytes > ctx->smem_limit) {
     // fall back to the exact need if the headroom does not fit
     want = (occ + 31) & ~31;
-    bytes = pair_smem_bytes(ctx->pc, want, ctx->ne_max);
+    pc = choose(want);
+    bytes = pair_smem_bytes(pc, want, ctx->ne_max);
     if (bytes > ctx->smem_limit) return EXAMD_ERR_CELL_OVERFLOW;
   }
+  ctx->pc.pack = pc.pack;
   ctx->cap = want;
   ctx->smem = bytes;
   // all variants used by this context

@@ -56,7 +56,7 @@ struct PairArgs {
 struct PairConfig {
   bool fp64 = false;
   bool multi = false;   // more than one atom type
-  bool kahan = true;    // compensated FP32 force sums (mixed)
+  bool pack = false;    // mixed form: compact per-warp tables (more CTAs per SM)
   bool energy = false;  // potential energy and virial
   bool count = false;   // candidate / accepted counters
   int warps = 8;
@@ -66,6 +66,8 @@ struct PairConfig {
 // needs (the mixed form's redo pass may need more).
 int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max);
 cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes);  // opt-in smem attribute
+// Resident CTAs per SM of the pair kernel at this capacity (occupancy calculator).
+int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max);
 cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st);
 cudaError_t upload_own_lut(const OwnLut& lut);
 

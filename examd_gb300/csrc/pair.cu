@@ -43,6 +43,8 @@
 // copy); the integrator sums an atom's 1..8 partials in a fixed order.
 #include <algorithm>
 
+#include <cuda_fp16.h>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "pairfn.cuh"
@@ -59,7 +61,7 @@ constexpr int kParts = 2;     // work units per 32 staged atoms (1, 3 and 4 meas
 constexpr float kFix = 32768.f;        // fixed-point scale 2^15
 constexpr float kFixInv = 1.f / 32768.f;
 constexpr float kFixMax = 1024.f;      // larger terms are left to the redo pass
-constexpr int kRedoBlocks = 304;       // grid of the redo pass (2 per SM)
+constexpr int kRedoBlocks = 152;       // grid of the redo pass (1 per SM)
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
@@ -69,9 +71,14 @@ struct Layout {
 };
 
 // Per-warp tables after the accepted-pair queues.  Mixed form: one step's
-// items by rank (float4 ptA + int4 ptB each) and the work unit's atoms by
-// rank (2 float4 each).  FP64 form: one step's items by lane (float4).
-constexpr int kWarpTabMixed = 32 * 16 + 32 * 16 + 32 * 32;
+// items by rank (ptA float4 + ptB) and the work unit's atoms by rank (btA
+// float4 + btB); wide: ptB int4, btB float4 of full values; compact: ptB
+// int2 with two 16-bit offsets, the atom's squared x-gaps as FP16 rounded
+// toward zero (so the pruning stays conservative) and btB int2.  The host
+// takes the compact tables where they fit more CTAs on an SM.  FP64 form: one
+// step's items by lane (float4).
+constexpr int kWarpTabWide = 32 * 16 + 32 * 16 + 32 * 16 + 32 * 16;
+constexpr int kWarpTabCompact = 32 * 16 + 32 * 8 + 32 * 16 + 32 * 8;
 constexpr int kWarpTabFp64 = 32 * 16;
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
@@ -79,7 +86,7 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 // redo: the mixed form's pass over tiles with large terms (fr: their FP32
 // sums, over the accepted-pair queues, which that pass does not use, when
 // they fit there).
-__host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int nw, bool redo = false) {
+__host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int nw, bool redo, bool pack) {
   Layout L;
   int o = 0;
   L.lstart = o; o = align16(o + 4 * (ne_max + 1));
@@ -93,7 +100,7 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.red = o;    o = align16(o + 8 * 8 * nw + 16);  // + the unit counter and the large-term flag
   L.r2l = o;    o = align16(o + (fp64 ? 64 * nw : 0));  // rank -> lane tables (FP64 form)
   L.lut = o;    o = align16(o + (int)sizeof(OwnLut));
-  const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64 : 20 * kQueue + kWarpTabMixed) * nw;
+  const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64 : 20 * kQueue + (pack ? kWarpTabCompact : kWarpTabWide)) * nw;
   L.queue = o;  o = align16(o + qbytes);
   L.pf = o;     o = align16(o + 16 * cap);
   if (fp64) {
@@ -113,8 +120,8 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
 }
 
 int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max) {
-  const int main = make_layout(cfg.fp64, cap, ne_max, cfg.warps).bytes;
-  return cfg.fp64 ? main : std::max(main, make_layout(false, cap, ne_max, cfg.warps, true).bytes);
+  const int main = make_layout(cfg.fp64, cap, ne_max, cfg.warps, false, cfg.pack).bytes;
+  return cfg.fp64 ? main : std::max(main, make_layout(false, cap, ne_max, cfg.warps, true, cfg.pack).bytes);
 }
 
 // Exact sum of FP32 terms in 64-bit fixed point (2^-32 resolution): the total
@@ -269,7 +276,7 @@ __device__ __forceinline__ void force_batch64(int cnt, const int* qk, const doub
 // over the tiles whose first pass met a large term; it recomputes the tile's
 // pairs, sums only the large terms (FP32 shared atomics) and adds them to the
 // outputs that the first pass wrote.
-template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, bool REDO>
+template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, bool REDO, bool PACK>
 __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned FULL = 0xffffffffu;
@@ -280,7 +287,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   const int tx = t1.x, ty = t1.y, tz = t1.z;
   const int EX = tx + 2, EY = ty + 2, EZ = tz + 2;
   const int NE = EX * EY * EZ;
-  const Layout L = make_layout(FP64, A.cap, A.ne_max, nw, REDO);
+  const Layout L = make_layout(FP64, A.cap, A.ne_max, nw, REDO, PACK);
   int* lstart = (int*)(smem + L.lstart);
   int* gfirst = (int*)(smem + L.gfirst);
   float* ox = (float*)(smem + L.ox);
@@ -448,10 +455,12 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   int* qk = (int*)(smem + L.queue + kQd * kQueue * nw) + warp * kQueue;
   // per-warp tables (kWarpTab*): one step's items (ptA, ptB) and, mixed
   // form, the work unit's atoms (bt)
-  unsigned char* wtab = smem + L.queue + (kQd + 4) * kQueue * nw + warp * (FP64 ? kWarpTabFp64 : kWarpTabMixed);
+  unsigned char* wtab =
+      smem + L.queue + (kQd + 4) * kQueue * nw + warp * (FP64 ? kWarpTabFp64 : (PACK ? kWarpTabCompact : kWarpTabWide));
   float4* ptA = (float4*)wtab;
-  int4* ptB = (int4*)(wtab + 32 * 16);
-  float4* bt = (float4*)(wtab + 32 * 32);
+  void* ptB = wtab + 32 * 16;
+  float4* btA = (float4*)(wtab + (PACK ? 32 * 24 : 32 * 32));
+  void* btB = wtab + (PACK ? 32 * 40 : 32 * 48);
   int qn = 0, qh = 0;  // queued pairs and the ring's head
   const unsigned lt = (1u << lane) - 1u;
   const unsigned le = FULL >> (31 - lane);
@@ -531,7 +540,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       // candidate k to its staged atom: m = k + (k < e1 ? o1 : o2)
       const int rk = __popc(hb & lt);
       ptA[rk] = make_float4(-pi.x, Cy, Cz, __int_as_float(i | (__float_as_int(pi.w) << 28)));
-      ptB[rk] = make_int4(lo1 - s0, s0 + n1, lo2 - n1 - s0, 0);
+      if (PACK)
+        ((int2*)ptB)[rk] = make_int2(((lo1 - s0) & 0xffff) | ((lo2 - n1 - s0) << 16), s0 + n1);
+      else
+        ((int4*)ptB)[rk] = make_int4(lo1 - s0, s0 + n1, lo2 - n1 - s0, 0);
     }
     __syncwarp();
     // distance tests; accepted pairs go to the queue
@@ -541,10 +553,21 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int qr = qb + __popc(M & le) - 1;  // >= 0: the first item starts at 0
       qb += __popc(M);
       const float4 a = ptA[qr];
-      const int4 b = ptB[qr];
+      int o1, e1, o2;
+      if (PACK) {
+        const int2 b = ((const int2*)ptB)[qr];
+        o1 = (int)(short)(b.x & 0xffff);
+        o2 = b.x >> 16;
+        e1 = b.y;
+      } else {
+        const int4 b = ((const int4*)ptB)[qr];
+        o1 = b.x;
+        e1 = b.y;
+        o2 = b.z;
+      }
       const int k = K + lane;
       const bool valid = k < T;
-      const int m = (k < b.y ? b.x : b.z) + k;
+      const int m = (k < e1 ? o1 : o2) + k;
       const float4 pj = pf[valid ? m : 0];
       float4 dq;
       dq.x = pj.x + a.x;
@@ -677,8 +700,16 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const unsigned wb = __ballot_sync(FULL, aw > 0);
       if (aw > 0) {  // the working atoms' data by rank (as0 < 512, ia < 2^14, acls < 128)
         const int rk = __popc(wb & lt);
-        bt[rk] = make_float4(apy, apz, am2, am1);
-        bt[32 + rk] = make_float4(ap1, ap2, __int_as_float(as0 | (ia << 9)), __int_as_float(cia | (acls << 15)));
+        const int wa = as0 | (ia << 9), wc = cia | (acls << 15);
+        if (PACK) {
+          const __half2 hm = __halves2half2(__float2half_rz(am2), __float2half_rz(am1));
+          const __half2 hp = __halves2half2(__float2half_rz(ap1), __float2half_rz(ap2));
+          btA[rk] = make_float4(apy, apz, *reinterpret_cast<const float*>(&hm), *reinterpret_cast<const float*>(&hp));
+          ((int2*)btB)[rk] = make_int2(wa, wc);
+        } else {
+          btA[rk] = make_float4(apy, apz, am2, am1);
+          ((float4*)btB)[rk] = make_float4(ap1, ap2, __int_as_float(wa), __int_as_float(wc));
+        }
       }
       __syncwarp();
       int qb = 0;  // working atoms that start before K
@@ -688,9 +719,29 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         qb += __popc(M);
         const int k = K + lane;
         const bool valid = k < W;
-        const float4 b0v = bt[qr], b1v = bt[32 + qr];
-        const float py = b0v.x, pz = b0v.y, xm2 = b0v.z, xm1 = b0v.w, xp1 = b1v.x, xp2 = b1v.y;
-        const int sq = __float_as_int(b1v.z), cc = __float_as_int(b1v.w);
+        const float4 b0v = btA[qr];
+        const float py = b0v.x, pz = b0v.y;
+        float xm2, xm1, xp1, xp2;
+        int sq, cc;
+        if (PACK) {
+          const float2 gm = __half22float2(*reinterpret_cast<const __half2*>(&b0v.z));
+          const float2 gp = __half22float2(*reinterpret_cast<const __half2*>(&b0v.w));
+          const int2 b1v = ((const int2*)btB)[qr];
+          xm2 = gm.x;
+          xm1 = gm.y;
+          xp1 = gp.x;
+          xp2 = gp.y;
+          sq = b1v.x;
+          cc = b1v.y;
+        } else {
+          const float4 b1v = ((const float4*)btB)[qr];
+          xm2 = b0v.z;
+          xm1 = b0v.w;
+          xp1 = b1v.x;
+          xp2 = b1v.y;
+          sq = __float_as_int(b1v.z);
+          cc = __float_as_int(b1v.w);
+        }
         const int s_q = sq & 511, i = sq >> 9;
         const int ci = cc & 0x7fff, cls = cc >> 15;
         const int lx = ci & 31, ly = (ci >> 5) & 31, lz = ci >> 10;
@@ -932,24 +983,24 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   }
 }
 
-template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
+template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, bool PACK>
 __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
-  pair_tile<FP64, MULTI, ENERGY, COUNT, false>(A, blockIdx.x);
+  pair_tile<FP64, MULTI, ENERGY, COUNT, false, PACK>(A, blockIdx.x);
 }
 
 // Mixed form: the redo pass over the tiles that k_pair listed (normally none,
 // and the blocks return at once).  The block that finishes last empties the
-// list; every block has read its length before any block counts itself done.
-template <bool MULTI>
+// list: every block has read its length (a read that its loop and barrier
+// depend on) before its thread 0 counts the block done.
+template <bool MULTI, bool PACK>
 __global__ void __launch_bounds__(256, 3) k_pair_redo(const PairArgs A) {
   const int n = *(volatile const int*)A.redo_n;
   for (int j = blockIdx.x; j < n; j += gridDim.x) {
-    pair_tile<false, MULTI, false, false, true>(A, A.redo[j]);
+    pair_tile<false, MULTI, false, false, true, PACK>(A, A.redo[j]);
     __syncthreads();
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
     if (atomicAdd(A.redo_done, 1u) == gridDim.x - 1) {
       *A.redo_n = 0;
       *A.redo_done = 0;
@@ -957,28 +1008,34 @@ __global__ void __launch_bounds__(256, 3) k_pair_redo(const PairArgs A) {
   }
 }
 
-template <bool FP64, bool MULTI, bool ENERGY, bool COUNT>
+template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, bool PACK>
 static void* kfn() {
-  return (void*)&k_pair<FP64, MULTI, ENERGY, COUNT>;
+  return (void*)&k_pair<FP64, MULTI, ENERGY, COUNT, PACK>;
 }
 
+// The FP64 form has one table layout (PACK = false).
 static void* pick(const PairConfig& c) {
-#define EXAMD_PICK(F, M)                                               \
-  if (c.energy && c.count) return kfn<F, M, true, true>();            \
-  if (c.energy) return kfn<F, M, true, false>();                      \
-  if (c.count) return kfn<F, M, false, true>();                       \
-  return kfn<F, M, false, false>();
+#define EXAMD_PICK(F, M, P)                                            \
+  if (c.energy && c.count) return kfn<F, M, true, true, P>();         \
+  if (c.energy) return kfn<F, M, true, false, P>();                   \
+  if (c.count) return kfn<F, M, false, true, P>();                    \
+  return kfn<F, M, false, false, P>();
   if (c.fp64) {
-    if (c.multi) { EXAMD_PICK(true, true) }
-    EXAMD_PICK(true, false)
+    if (c.multi) { EXAMD_PICK(true, true, false) }
+    EXAMD_PICK(true, false, false)
   }
-  if (c.multi) { EXAMD_PICK(false, true) }
-  EXAMD_PICK(false, false)
+  if (c.pack) {
+    if (c.multi) { EXAMD_PICK(false, true, true) }
+    EXAMD_PICK(false, false, true)
+  }
+  if (c.multi) { EXAMD_PICK(false, true, false) }
+  EXAMD_PICK(false, false, false)
 #undef EXAMD_PICK
 }
 
 static void* pick_redo(const PairConfig& c) {
-  return c.multi ? (void*)&k_pair_redo<true> : (void*)&k_pair_redo<false>;
+  if (c.pack) return c.multi ? (void*)&k_pair_redo<true, true> : (void*)&k_pair_redo<false, true>;
+  return c.multi ? (void*)&k_pair_redo<true, false> : (void*)&k_pair_redo<false, false>;
 }
 
 cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes) {
@@ -987,17 +1044,25 @@ cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes) {
   return cudaFuncSetAttribute(pick_redo(cfg), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
 }
 
+int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max) {
+  const int smem = make_layout(cfg.fp64, cap, ne_max, cfg.warps, false, cfg.pack).bytes;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pick(cfg), 32 * cfg.warps, (size_t)smem) != cudaSuccess)
+    return 0;
+  return n;
+}
+
 cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st) {
   if (ntiles <= 0) return cudaSuccess;
   void* fn = pick(cfg);
   void* args[] = {(void*)&a};
   // smem_bytes (the larger of the two passes' needs) bounds both launches
-  const int main_smem = make_layout(cfg.fp64, a.cap, a.ne_max, cfg.warps).bytes;
+  const int main_smem = make_layout(cfg.fp64, a.cap, a.ne_max, cfg.warps, false, cfg.pack).bytes;
   if (main_smem > smem_bytes) return cudaErrorInvalidValue;
   cudaError_t e = cudaLaunchKernel(fn, dim3(ntiles), dim3(32 * cfg.warps), args, (size_t)main_smem, st);
   if (e != cudaSuccess || cfg.fp64) return e;
   // the redo pass: a few blocks per SM at most; nothing to do in a thermal system
-  const int redo_smem = make_layout(false, a.cap, a.ne_max, cfg.warps, true).bytes;
+  const int redo_smem = make_layout(false, a.cap, a.ne_max, cfg.warps, true, cfg.pack).bytes;
   if (redo_smem > smem_bytes) return cudaErrorInvalidValue;
   return cudaLaunchKernel(pick_redo(cfg), dim3(std::min(ntiles, kRedoBlocks)), dim3(32 * cfg.warps), args,
                           (size_t)redo_smem, st);

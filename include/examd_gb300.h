@@ -86,6 +86,8 @@ typedef struct examd_params {
                       /* 0: they are wrapped periodically                     */
   int device;         /* CUDA device ordinal                                  */
   int potential;      /* EXAMD_POT_*                                          */
+  int pair_tables;    /* mixed form's per-warp tables in the pair kernel:     */
+                      /* 0 = chosen by occupancy, 1 = wide, 2 = compact       */
 } examd_params;
 
 /* One independent periodic box of a batched ensemble. */
