@@ -514,7 +514,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   // while another finishes a long j-range.  A lane finds its item from the
   // bitmask of the items that start in the current 32 candidates, and reads
   // the item's data from the per-warp tables by its rank.
-  auto consume = [&](int i, int r, int lo1, int n1, int lo2, int n2) {
+  auto consume = [&](int i, float cy, float cz, int lo1, int n1, int lo2, int n2) {
     const int nt = n1 + n2;
     const unsigned hb = __ballot_sync(FULL, nt > 0);
     if (hb == 0u) return;
@@ -529,17 +529,12 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     const int T = __shfl_sync(FULL, incl, 31);
     if (nt > 0) {
       // the atom's position moved into the j-cells' frame: d = x_j + C
-      // (y, z relative to the cell origin)
+      // (y, z relative to the cell origin; cy, cz: the j-row's origin offset)
       const float4 pi = pf[i];
-      const int ci = code[i];
-      const int ly = (ci >> 5) & 31, lz = ci >> 10;
-      const int dy = srows[2 * r], dz = srows[2 * r + 1];
-      const float Cy = dyt[ly * kDT + dy + 2] - pi.y;
-      const float Cz = dzt[lz * kDT + dz + 2] - pi.z;
       // by rank: the item's key base and frame shift, and the offsets that map
       // candidate k to its staged atom: m = k + (k < e1 ? o1 : o2)
       const int rk = __popc(hb & lt);
-      ptA[rk] = make_float4(-pi.x, Cy, Cz, __int_as_float(i | (__float_as_int(pi.w) << 28)));
+      ptA[rk] = make_float4(-pi.x, cy - pi.y, cz - pi.z, __int_as_float(MULTI ? i | (__float_as_int(pi.w) << 28) : i));
       if (PACK)
         ((int2*)ptB)[rk] = make_int2(((lo1 - s0) & 0xffff) | ((lo2 - n1 - s0) << 16), s0 + n1);
       else
@@ -578,10 +573,11 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int kb = __float_as_int(a.w);
       if (COUNT && valid) ++neval;
       const float thr = MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
+      const int key = MULTI ? kb | (m << 14) | (tj << 30) : kb | (m << 14);
       if (REDO)
-        redo_pair(valid && dq.w <= thr, dq, kb | (m << 14) | (tj << 30));
+        redo_pair(valid && dq.w <= thr, dq, key);
       else
-        enqueue(valid && dq.w <= thr, dq, kb | (m << 14) | (tj << 30));
+        enqueue(valid && dq.w <= thr, dq, key);
     }
     __syncwarp();
   };
@@ -751,9 +747,12 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
           mask = sown->lut[cls][r];
         }
         int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
+        float cy = 0.f, cz = 0.f;
         if (mask) {
           const int dy = srows[2 * r], dz = srows[2 * r + 1];
           const int rowbase = ((ly + dy) + EY * (lz + dz)) * EX + lx - 2;  // + bit b -> ext cell of dx = b - 2
+          cy = dyt[ly * kDT + dy + 2];
+          cz = dzt[lz * kDT + dz + 2];
           if (COUNT) {  // every atom of the owned cells, as the reference visits them
             for (int b = 0; b < 5; ++b)
               if ((mask >> b) & 1) {
@@ -793,7 +792,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
             }
           }
         }
-        consume(i, r, lo1, n1, lo2, n2);
+        consume(i, cy, cz, lo1, n1, lo2, n2);
       }
       __syncwarp();
     }
