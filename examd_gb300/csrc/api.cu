@@ -136,6 +136,7 @@ struct examd_ctx {
   LJTable lj{};
   PairConfig pc;
   int cap = 0, smem = 0, smem_limit = 0;
+  int cap_redo = 0;     // mixed form: staged-atom capacity of the redo pass
   int pair_tables = 0;  // examd_params.pair_tables
   int dev = 0;
   cudaStream_t st = nullptr;
@@ -744,7 +745,10 @@ int check_status(examd_ctx* ctx) {
   return take_status(ctx);
 }
 
-// Staged-atom capacity of a tile from the current binning (+25% + 64 headroom).
+// Staged-atom capacities of a tile from the current binning: +25% + 64
+// headroom for the FP64 form and for the mixed form's redo pass; +6% + 32 for
+// the mixed form's first pass (a tile that outgrows it before the next update
+// is computed in full by the redo pass, at the redo capacity).
 int update_capacity(examd_ctx* ctx) {
   CK(cudaMemsetAsync(ctx->d_occ, 0, 2 * sizeof(int), ctx->st));
   k_tile_occupancy<<<ctx->ntiles, 128, 0, ctx->st>>>(ctx->d_tiles, ctx->d_boxes, ctx->cstart, ctx->d_occ);
@@ -752,7 +756,8 @@ int update_capacity(examd_ctx* ctx) {
   int occ = 0;
   CK(cudaMemcpyAsync(&occ, ctx->d_occ, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
-  int want = ((occ + occ / 4 + 64) + 31) & ~31;
+  int want_r = std::max(((occ + occ / 4 + 64) + 31) & ~31, ctx->cap_redo);
+  int want = ctx->pc.fp64 ? want_r : ((occ + occ / 16 + 32) + 31) & ~31;
   if (want <= ctx->cap) return EXAMD_OK;
   // mixed form with pair_tables = 0: the compact per-warp tables where they
   // fit more CTAs on an SM at this capacity (or where only they fit at all)
@@ -766,21 +771,22 @@ int update_capacity(examd_ctx* ctx) {
       PairConfig q = e ? k : w;
       if (pair_prepare(q, ctx->smem_limit) != cudaSuccess) return c;
     }
-    c.pack = pair_smem_bytes(w, cap, ctx->ne_max) > ctx->smem_limit ||
+    c.pack = pair_smem_bytes(w, cap, want_r, ctx->ne_max) > ctx->smem_limit ||
              pair_blocks_per_sm(k, cap, ctx->ne_max) > pair_blocks_per_sm(w, cap, ctx->ne_max);
     return c;
   };
   PairConfig pc = choose(want);
-  int bytes = pair_smem_bytes(pc, want, ctx->ne_max);
+  int bytes = pair_smem_bytes(pc, want, want_r, ctx->ne_max);
   if (bytes > ctx->smem_limit) {
     // fall back to the exact need if the headroom does not fit
-    want = (occ + 31) & ~31;
+    want = want_r = (occ + 31) & ~31;
     pc = choose(want);
-    bytes = pair_smem_bytes(pc, want, ctx->ne_max);
+    bytes = pair_smem_bytes(pc, want, want_r, ctx->ne_max);
     if (bytes > ctx->smem_limit) return EXAMD_ERR_CELL_OVERFLOW;
   }
   ctx->pc.pack = pc.pack;
   ctx->cap = want;
+  ctx->cap_redo = want_r;
   ctx->smem = bytes;
   // all variants used by this context
   PairConfig c = ctx->pc;
@@ -810,6 +816,7 @@ PairArgs pair_args(examd_ctx* ctx) {
   a.tileC = ctx->tileC;
   a.status = ctx->status;
   a.cap = ctx->cap;
+  a.cap_redo = ctx->cap_redo;
   a.ne_max = ctx->ne_max;
   a.lj = ctx->lj;
   a.redo = ctx->redo;

@@ -43,7 +43,8 @@ struct PairArgs {
   double* tileW;     // per tile virial
   long long* tileC;  // per tile (candidates, accepted)
   int* status;
-  int cap;     // staged-atom capacity of a tile
+  int cap;     // staged-atom capacity of a tile (mixed form: of the first pass)
+  int cap_redo;  // mixed form: capacity of the redo pass
   int ne_max;  // largest ext-cell count of a tile
   LJTable lj;
   // mixed form: tiles whose pair-force terms exceeded the fixed-point range,
@@ -62,9 +63,9 @@ struct PairConfig {
   int warps = 8;
 };
 
-// Dynamic shared memory for a tile capacity: the larger of the two passes'
-// needs (the mixed form's redo pass may need more).
-int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max);
+// Dynamic shared memory for the tile capacities: the larger of the first
+// pass's need at cap and, mixed form, the redo pass's at cap_redo.
+int pair_smem_bytes(const PairConfig& cfg, int cap, int cap_redo, int ne_max);
 cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes);  // opt-in smem attribute
 // Resident CTAs per SM of the pair kernel at this capacity (occupancy calculator).
 int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max);

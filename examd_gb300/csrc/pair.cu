@@ -62,6 +62,12 @@ constexpr float kFix = 32768.f;        // fixed-point scale 2^15
 constexpr float kFixInv = 1.f / 32768.f;
 constexpr float kFixMax = 1024.f;      // larger terms are left to the redo pass
 constexpr int kRedoBlocks = 152;       // grid of the redo pass (1 per SM)
+// Passes of the mixed form's tile body: the first pass; the redo pass's two
+// kinds of tile, one whose large terms were left out (only those are summed
+// and added) and one that overflowed the first pass's capacity (computed in
+// full at the redo capacity, large terms in an FP32 side array).
+constexpr int kMain = 0, kRedoBig = 1, kRedoFull = 2;
+constexpr int kFullBit = 1 << 30;      // redo-list entry: tile | kFullBit for an overflowed tile
 constexpr int kSeg = 4;                // lanes per segment of the i-side force sums
 
 // Shared-memory carve-up, identical on host and device.
@@ -84,10 +90,10 @@ constexpr int kWarpTabFp64 = 32 * 16;
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
-// redo: the mixed form's pass over tiles with large terms (fr: their FP32
-// sums, over the accepted-pair queues, which that pass does not use, when
-// they fit there).
-__host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int nw, bool redo, bool pack) {
+// mode: kMain, kRedoBig (fr: the large terms' FP32 sums, over the
+// accepted-pair queues, which that pass does not use, when they fit there)
+// or kRedoFull (fr after everything else).
+__host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int nw, int mode, bool pack) {
   Layout L;
   int o = 0;
   L.lstart = o; o = align16(o + 4 * (ne_max + 1));
@@ -113,16 +119,21 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   }
   L.code = o;   o = align16(o + 2 * cap);
   L.fr = L.queue;
-  if (redo && !fp64 && 3 * 4 * cap > 20 * kQueue * nw) {
+  if (!fp64 && (mode == kRedoFull || (mode == kRedoBig && 3 * 4 * cap > 20 * kQueue * nw))) {
     L.fr = o;   o = align16(o + 3 * 4 * cap);
   }
   L.bytes = o;
   return L;
 }
 
-int pair_smem_bytes(const PairConfig& cfg, int cap, int ne_max) {
-  const int main = make_layout(cfg.fp64, cap, ne_max, cfg.warps, false, cfg.pack).bytes;
-  return cfg.fp64 ? main : std::max(main, make_layout(false, cap, ne_max, cfg.warps, true, cfg.pack).bytes);
+static int redo_smem_bytes(const PairConfig& cfg, int cap_redo, int ne_max) {
+  return std::max(make_layout(false, cap_redo, ne_max, cfg.warps, kRedoBig, cfg.pack).bytes,
+                  make_layout(false, cap_redo, ne_max, cfg.warps, kRedoFull, cfg.pack).bytes);
+}
+
+int pair_smem_bytes(const PairConfig& cfg, int cap, int cap_redo, int ne_max) {
+  const int main = make_layout(cfg.fp64, cap, ne_max, cfg.warps, kMain, cfg.pack).bytes;
+  return cfg.fp64 ? main : std::max(main, redo_smem_bytes(cfg, cap_redo, ne_max));
 }
 
 // Exact sum of FP32 terms in 64-bit fixed point (2^-32 resolution): the total
@@ -154,12 +165,12 @@ struct FixSum {
 // A pair-force term too large for the fixed-point sums (a component of
 // magnitude >= kFixMax, i.e. r < ~0.79 sigma at eps = 1, which thermal
 // configurations do not reach) is left out here and raises the tile's flag
-// (*big_flag); the redo pass adds it.
-template <bool MULTI, bool ENERGY, bool COUNT>
-__device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, const int* qk, int* fa,
-                                            const PairArgs& A, FixSum& ek, FixSum& wk, int& nacc,
+// (*big_flag); the redo pass adds it.  SIDE (the full redo pass): such terms
+// go to the FP32 side sums fr instead.
+template <bool MULTI, bool ENERGY, bool COUNT, bool SIDE>
+__device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, const int* qk, int* fa, float* fr,
+                                            int cap, const PairArgs& A, FixSum& ek, FixSum& wk, int& nacc,
                                             int* big_flag) {
-  const int cap = A.cap;
   const LJTable& lj = A.lj;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -201,7 +212,18 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, c
     atomicAdd(&fa[cap + m], -iy);
     atomicAdd(&fa[2 * cap + m], -iz);
   }
-  if (big) *big_flag = 1;
+  if (big) {
+    if (SIDE) {
+      atomicAdd(&fr[i], fx * kFixInv);
+      atomicAdd(&fr[cap + i], fy * kFixInv);
+      atomicAdd(&fr[2 * cap + i], fz * kFixInv);
+      atomicAdd(&fr[m], -fx * kFixInv);
+      atomicAdd(&fr[cap + m], -fy * kFixInv);
+      atomicAdd(&fr[2 * cap + m], -fz * kFixInv);
+    } else {
+      *big_flag = 1;
+    }
+  }
   // i side: sum over runs of equal i (inactive lanes form one run with i = -1),
   // in segments of kSeg lanes from the run's first one: each segment's last
   // lane adds the segment's total (4: measured against 2, 8 and 16)
@@ -273,11 +295,15 @@ __device__ __forceinline__ void force_batch64(int cnt, const int* qk, const doub
   }
 }
 
-// One tile.  REDO (mixed form only, without energy or counters): the pass
-// over the tiles whose first pass met a large term; it recomputes the tile's
-// pairs, sums only the large terms (FP32 shared atomics) and adds them to the
-// outputs that the first pass wrote.
-template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, bool REDO, bool PACK>
+// One tile.  MODE (mixed form; the FP64 form has only kMain):
+// - kMain: the first pass, at capacity A.cap; a tile with more staged atoms
+//   is listed for a full redo, one with a large term for a large-term redo;
+// - kRedoBig (without energy or counters): recomputes the tile's pairs, sums
+//   only the large terms (FP32 shared atomics) and adds them to the outputs
+//   that the first pass wrote;
+// - kRedoFull: the whole tile at capacity A.cap_redo, large terms in FP32
+//   side sums, outputs, energy and counters written as the first pass would.
+template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, int MODE, bool PACK>
 __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned FULL = 0xffffffffu;
@@ -288,7 +314,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   const int tx = t1.x, ty = t1.y, tz = t1.z;
   const int EX = tx + 2, EY = ty + 2, EZ = tz + 2;
   const int NE = EX * EY * EZ;
-  const Layout L = make_layout(FP64, A.cap, A.ne_max, nw, REDO, PACK);
+  const int cap = MODE == kMain ? A.cap : A.cap_redo;
+  const Layout L = make_layout(FP64, cap, A.ne_max, nw, MODE, PACK);
   int* lstart = (int*)(smem + L.lstart);
   int* gfirst = (int*)(smem + L.gfirst);
   float* ox = (float*)(smem + L.ox);
@@ -302,7 +329,6 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   const signed char* srows = &sown->rows[0][0];
   float4* pf = (float4*)(smem + L.pf);
   unsigned short* code = (unsigned short*)(smem + L.code);
-  const int cap = A.cap;
 
   // (1) ext cells: global cell, count, first atom; ownership tables to smem
   for (int e = tid; e < NE; e += blockDim.x) {
@@ -389,6 +415,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     __syncthreads();
   }
   const int total = lstart[NE];
+  if (!FP64 && MODE == kMain && total > cap) {  // the redo pass computes it at its capacity
+    if (tid == 0) A.redo[atomicAdd(A.redo_n, 1)] = tile | kFullBit;
+    return;
+  }
   if (total > cap) {
     if (tid == 0) {
       atomicOr(A.status, ST_OVERFLOW);
@@ -427,10 +457,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         pf[t] = make_float4(ox[lx] + u.x, u.y, u.z, u.w);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          if (REDO)
-            fr[c * cap + t] = 0.f;
-          else
-            fa[c * cap + t] = 0;
+          if (MODE != kMain) fr[c * cap + t] = 0.f;
+          if (MODE != kRedoBig) fa[c * cap + t] = 0;
         }
       }
       code[t] = cc;
@@ -482,7 +510,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
                                             qh);
       else
-        force_batch<MULTI, ENERGY, COUNT>(32, qh, qd, qk, fa, A, ek, wk, nacc, big_flag);
+        force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(32, qh, qd, qk, fa, fr, cap, A, ek, wk, nacc, big_flag);
       __syncwarp();
       qh = (qh + 32) & (kQueue - 1);
       qn -= 32;
@@ -575,7 +603,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       if (COUNT && valid) ++neval;
       const float thr = MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
       const int key = MULTI ? kb | (m << 14) | (tj << 30) : kb | (m << 14);
-      if (REDO)
+      if (MODE == kRedoBig)
         redo_pair(valid && dq.w <= thr, dq, key);
       else
         enqueue(valid && dq.w <= thr, dq, key);
@@ -883,11 +911,11 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
                                           qh);
     else
-      force_batch<MULTI, ENERGY, COUNT>(qn, qh, qd, qk, fa, A, ek, wk, nacc, big_flag);
+      force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(qn, qh, qd, qk, fa, fr, cap, A, ek, wk, nacc, big_flag);
   }
   __syncthreads();
   // a large term was left out: list the tile for the redo pass
-  if (!FP64 && !REDO && tid == 0 && *big_flag) A.redo[atomicAdd(A.redo_n, 1)] = tile;
+  if (!FP64 && MODE == kMain && tid == 0 && *big_flag) A.redo[atomicAdd(A.redo_n, 1)] = tile;
 
   // (4) write-back: home atoms -> Fown, halo copies -> P[slot]
   for (int t = tid; t < total; t += blockDim.x) {
@@ -903,7 +931,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       for (int c = 0; c < 3; ++c) F[c * A.N + g] = fd[c * cap + t];
     } else {
       float4* F = slot == 0 ? (float4*)A.Fown : (float4*)A.P + (size_t)(slot - 1) * A.N;
-      if (REDO) {
+      if (MODE == kRedoBig) {
         // this copy's output was written by the first pass and by this tile
         // only (a copy's slot pattern is unique to one tile)
         const float x = fr[t], y = fr[cap + t], z = fr[2 * cap + t];
@@ -917,7 +945,9 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       } else {
         float f[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) f[c] = (float)fa[c * cap + t] * kFixInv;
+        for (int c = 0; c < 3; ++c)
+          f[c] = MODE == kRedoFull ? fmaf((float)fa[c * cap + t], kFixInv, fr[c * cap + t])
+                                   : (float)fa[c * cap + t] * kFixInv;
         F[g] = make_float4(f[0], f[1], f[2], 0.f);
       }
     }
@@ -985,18 +1015,22 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
 
 template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, bool PACK>
 __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
-  pair_tile<FP64, MULTI, ENERGY, COUNT, false, PACK>(A, blockIdx.x);
+  pair_tile<FP64, MULTI, ENERGY, COUNT, kMain, PACK>(A, blockIdx.x);
 }
 
 // Mixed form: the redo pass over the tiles that k_pair listed (normally none,
 // and the blocks return at once).  The block that finishes last empties the
 // list: every block has read its length (a read that its loop and barrier
 // depend on) before its thread 0 counts the block done.
-template <bool MULTI, bool PACK>
+template <bool MULTI, bool PACK, bool ENERGY, bool COUNT>
 __global__ void __launch_bounds__(256, 3) k_pair_redo(const PairArgs A) {
   const int n = *(volatile const int*)A.redo_n;
   for (int j = blockIdx.x; j < n; j += gridDim.x) {
-    pair_tile<false, MULTI, false, false, true, PACK>(A, A.redo[j]);
+    const int w = A.redo[j];
+    if (w & kFullBit)
+      pair_tile<false, MULTI, ENERGY, COUNT, kRedoFull, PACK>(A, w & ~kFullBit);
+    else
+      pair_tile<false, MULTI, false, false, kRedoBig, PACK>(A, w);
     __syncthreads();
   }
   __syncthreads();
@@ -1033,9 +1067,17 @@ static void* pick(const PairConfig& c) {
 #undef EXAMD_PICK
 }
 
+template <bool MULTI, bool PACK>
+static void* pick_redo_ec(const PairConfig& c) {
+  if (c.energy && c.count) return (void*)&k_pair_redo<MULTI, PACK, true, true>;
+  if (c.energy) return (void*)&k_pair_redo<MULTI, PACK, true, false>;
+  if (c.count) return (void*)&k_pair_redo<MULTI, PACK, false, true>;
+  return (void*)&k_pair_redo<MULTI, PACK, false, false>;
+}
+
 static void* pick_redo(const PairConfig& c) {
-  if (c.pack) return c.multi ? (void*)&k_pair_redo<true, true> : (void*)&k_pair_redo<false, true>;
-  return c.multi ? (void*)&k_pair_redo<true, false> : (void*)&k_pair_redo<false, false>;
+  if (c.pack) return c.multi ? pick_redo_ec<true, true>(c) : pick_redo_ec<false, true>(c);
+  return c.multi ? pick_redo_ec<true, false>(c) : pick_redo_ec<false, false>(c);
 }
 
 cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes) {
@@ -1045,7 +1087,7 @@ cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes) {
 }
 
 int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max) {
-  const int smem = make_layout(cfg.fp64, cap, ne_max, cfg.warps, false, cfg.pack).bytes;
+  const int smem = make_layout(cfg.fp64, cap, ne_max, cfg.warps, kMain, cfg.pack).bytes;
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pick(cfg), 32 * cfg.warps, (size_t)smem) != cudaSuccess)
     return 0;
@@ -1057,12 +1099,12 @@ cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, in
   void* fn = pick(cfg);
   void* args[] = {(void*)&a};
   // smem_bytes (the larger of the two passes' needs) bounds both launches
-  const int main_smem = make_layout(cfg.fp64, a.cap, a.ne_max, cfg.warps, false, cfg.pack).bytes;
+  const int main_smem = make_layout(cfg.fp64, a.cap, a.ne_max, cfg.warps, kMain, cfg.pack).bytes;
   if (main_smem > smem_bytes) return cudaErrorInvalidValue;
   cudaError_t e = cudaLaunchKernel(fn, dim3(ntiles), dim3(32 * cfg.warps), args, (size_t)main_smem, st);
   if (e != cudaSuccess || cfg.fp64) return e;
   // the redo pass: a few blocks per SM at most; nothing to do in a thermal system
-  const int redo_smem = make_layout(false, a.cap, a.ne_max, cfg.warps, true, cfg.pack).bytes;
+  const int redo_smem = redo_smem_bytes(cfg, a.cap_redo, a.ne_max);
   if (redo_smem > smem_bytes) return cudaErrorInvalidValue;
   return cudaLaunchKernel(pick_redo(cfg), dim3(std::min(ntiles, kRedoBlocks)), dim3(32 * cfg.warps), args,
                           (size_t)redo_smem, st);

@@ -66,3 +66,48 @@ def test_every_atom_in_close_pairs(gpulib):
     assert e[0] == pytest.approx(e64, rel=1e-5)
     # the large terms' FP32 sums are the only order-dependent part
     assert np.abs(f32b - f32).max() / frms <= 1e-6
+
+
+def test_first_pass_overflow_goes_to_the_redo_pass(gpulib):
+    """The mixed form's first pass holds the largest tile at binning time plus
+    6 % + 32 atoms; new positions through forces_at (no capacity update) that
+    pack more atoms into a tile send that tile to the redo pass, which
+    computes it in full at its own capacity (+25 % + 64).  A sine compression
+    along z (pairs down to ~0.65 sigma) does that to the densest tiles: its
+    amplitude is the first one whose largest tile falls between the two
+    capacities.  Forces and energy match the FP64 form."""
+    from examd_gb300 import workloads as W
+    c = W.liquid_fcc(16)  # 16,384 atoms
+    L = np.asarray(c["boxes"][0], dtype=np.float64)
+    pos = c["pos"]
+
+    def squeeze(a):
+        p = pos.copy()
+        z = pos[:, 2]
+        p[:, 2] = (z - a * L[2] / (2 * np.pi) * np.sin(2 * np.pi * z / L[2])) % L[2]
+        return p
+
+    def largest_tile(p):
+        with gpulib.MidpointLJ(L, [len(p)], precision="mixed", rc=2.5) as s:
+            s.set_atoms(p)
+            return s.counters()["max_tile_atoms"]
+
+    occ_a = largest_tile(pos)
+    cap_first = (occ_a + occ_a // 16 + 32 + 31) // 32 * 32
+    cap_redo = (occ_a + occ_a // 4 + 64 + 31) // 32 * 32
+    posb = None
+    for a in (0.25, 0.3, 0.35, 0.4, 0.45, 0.5):
+        if cap_first < largest_tile(squeeze(a)) <= cap_redo:
+            posb = squeeze(a)
+            break
+    assert posb is not None
+    with gpulib.MidpointLJ(L, [len(pos)], precision="mixed", rc=2.5) as s:
+        s.set_atoms(pos)
+        f32, e32, _ = s.forces_at(posb, energy=True)
+    f64, e64 = forces(gpulib, posb, L, "fp64")
+    frms = np.sqrt((f64 * f64).sum(1).mean())
+    err = np.sqrt(((f32 - f64) ** 2).sum(1))
+    assert np.sqrt((err * err).mean()) / frms <= 1e-5
+    # the largest errors: the closest pairs' r^-13 terms with an FP32 separation
+    assert err.max() / frms <= 1e-4
+    assert e32[0] == pytest.approx(e64, rel=1e-5)
