@@ -131,7 +131,7 @@ struct examd_ctx {
   std::vector<int> tile0;  // nboxes + 1
   std::vector<int64_t> atom0;
   int64_t N = 0;
-  int NC = 0, ntiles = 0, ne_max = 0;
+  int NC = 0, ntiles = 0, ne_max = 0, ext_max = 0;
   double bl = 0.0;
   LJTable lj{};
   PairConfig pc;
@@ -514,6 +514,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
           tiles.push_back(d0);
           tiles.push_back(d1);
           ctx->ne_max = std::max(ctx->ne_max, (d1.x + 2) * (d1.y + 2) * (d1.z + 2));
+          ctx->ext_max = std::max(ctx->ext_max, std::max(d1.x, std::max(d1.y, d1.z)) + 2);
         }
     // boundary mask per cell: first or last cell of its tile on each axis
     std::vector<unsigned char> edge[3];
@@ -756,8 +757,8 @@ int update_capacity(examd_ctx* ctx) {
   int occ = 0;
   CK(cudaMemcpyAsync(&occ, ctx->d_occ, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
-  int want_r = std::max(((occ + occ / 4 + 64) + 31) & ~31, ctx->cap_redo);
-  int want = ctx->pc.fp64 ? want_r : ((occ + occ / 16 + 32) + 31) & ~31;
+  int want_r = std::max(((occ + occ / 4 + 64) + 7) & ~7, ctx->cap_redo);
+  int want = ctx->pc.fp64 ? want_r : ((occ + occ / 16 + 32) + 7) & ~7;
   if (want <= ctx->cap) return EXAMD_OK;
   // mixed form with pair_tables = 0: the compact per-warp tables where they
   // fit more CTAs on an SM at this capacity (or where only they fit at all)
@@ -771,17 +772,17 @@ int update_capacity(examd_ctx* ctx) {
       PairConfig q = e ? k : w;
       if (pair_prepare(q, ctx->smem_limit) != cudaSuccess) return c;
     }
-    c.pack = pair_smem_bytes(w, cap, want_r, ctx->ne_max) > ctx->smem_limit ||
-             pair_blocks_per_sm(k, cap, ctx->ne_max) > pair_blocks_per_sm(w, cap, ctx->ne_max);
+    c.pack = pair_smem_bytes(w, cap, want_r, ctx->ne_max, ctx->ext_max) > ctx->smem_limit ||
+             pair_blocks_per_sm(k, cap, ctx->ne_max, ctx->ext_max) > pair_blocks_per_sm(w, cap, ctx->ne_max, ctx->ext_max);
     return c;
   };
   PairConfig pc = choose(want);
-  int bytes = pair_smem_bytes(pc, want, want_r, ctx->ne_max);
+  int bytes = pair_smem_bytes(pc, want, want_r, ctx->ne_max, ctx->ext_max);
   if (bytes > ctx->smem_limit) {
     // fall back to the exact need if the headroom does not fit
-    want = want_r = (occ + 31) & ~31;
+    want = want_r = (occ + 7) & ~7;
     pc = choose(want);
-    bytes = pair_smem_bytes(pc, want, want_r, ctx->ne_max);
+    bytes = pair_smem_bytes(pc, want, want_r, ctx->ne_max, ctx->ext_max);
     if (bytes > ctx->smem_limit) return EXAMD_ERR_CELL_OVERFLOW;
   }
   ctx->pc.pack = pc.pack;
@@ -818,6 +819,7 @@ PairArgs pair_args(examd_ctx* ctx) {
   a.cap = ctx->cap;
   a.cap_redo = ctx->cap_redo;
   a.ne_max = ctx->ne_max;
+  a.ext_max = ctx->ext_max;
   a.lj = ctx->lj;
   a.redo = ctx->redo;
   a.redo_n = ctx->redo_n;

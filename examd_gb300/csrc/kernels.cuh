@@ -46,6 +46,7 @@ struct PairArgs {
   int cap;     // staged-atom capacity of a tile (mixed form: of the first pass)
   int cap_redo;  // mixed form: capacity of the redo pass
   int ne_max;  // largest ext-cell count of a tile
+  int ext_max;  // largest ext extent of a tile on one axis
   LJTable lj;
   // mixed form: tiles whose pair-force terms exceeded the fixed-point range,
   // for the redo pass (ntiles entries; count and done counter zero between launches)
@@ -65,10 +66,10 @@ struct PairConfig {
 
 // Dynamic shared memory for the tile capacities: the larger of the first
 // pass's need at cap and, mixed form, the redo pass's at cap_redo.
-int pair_smem_bytes(const PairConfig& cfg, int cap, int cap_redo, int ne_max);
+int pair_smem_bytes(const PairConfig& cfg, int cap, int cap_redo, int ne_max, int ext_max);
 cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes);  // opt-in smem attribute
 // Resident CTAs per SM of the pair kernel at this capacity (occupancy calculator).
-int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max);
+int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max, int ext_max);
 cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st);
 cudaError_t upload_own_lut(const OwnLut& lut);
 

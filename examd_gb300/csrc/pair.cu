@@ -72,7 +72,7 @@ constexpr int kSeg = 4;                // lanes per segment of the i-side force 
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
-  int lstart, gfirst, ox, oy, oz, dyt, dzt, img, red, r2l, lut, queue;
+  int lstart, gfirst, ox, oy, oz, dyt, dzt, img, cw, r2l, lut, queue;
   int pf, fa, px, code, fr;
   int bytes;
 };
@@ -93,18 +93,20 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 // mode: kMain, kRedoBig (fr: the large terms' FP32 sums, over the
 // accepted-pair queues, which that pass does not use, when they fit there)
 // or kRedoFull (fr after everything else).
-__host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int nw, int mode, bool pack) {
+// ne_max, ext_max: the largest tile's ext cells and ext extent on one axis.
+__host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int ext_max, int nw, int mode,
+                                              bool pack) {
   Layout L;
   int o = 0;
-  L.lstart = o; o = align16(o + 4 * (ne_max + 1));
+  L.lstart = o; o = align16(o + 2 * (ne_max + 1));  // < 2^16: at most the capacity
   L.gfirst = o; o = align16(o + 4 * ne_max);
-  L.ox = o;     o = align16(o + 4 * (kMaxExt + 1));
-  L.oy = o;     o = align16(o + 4 * (kMaxExt + 1));
-  L.oz = o;     o = align16(o + 4 * (kMaxExt + 1));
-  L.dyt = o;    o = align16(o + 4 * kMaxExt * kDT);
-  L.dzt = o;    o = align16(o + 4 * kMaxExt * kDT);
+  L.ox = o;     o = align16(o + 4 * (ext_max + 1));
+  L.oy = o;     o = align16(o + 4 * (ext_max + 1));
+  L.oz = o;     o = align16(o + 4 * (ext_max + 1));
+  L.dyt = o;    o = align16(o + 4 * ext_max * kDT);
+  L.dzt = o;    o = align16(o + 4 * ext_max * kDT);
   L.img = o;    o = align16(o + (fp64 ? 3 * 32 : 0));  // periodic image per ext coordinate (FP64 form)
-  L.red = o;    o = align16(o + 8 * 8 * nw + 16);  // + the unit counter and the large-term flag
+  L.cw = o;     o = align16(o + 16);  // unit counter, large-term flag, staged-atom total
   L.r2l = o;    o = align16(o + (fp64 ? 64 * nw : 0));  // rank -> lane tables (FP64 form)
   L.lut = o;    o = align16(o + (int)sizeof(OwnLut));
   const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64 : 20 * kQueue + (pack ? kWarpTabCompact : kWarpTabWide)) * nw;
@@ -126,14 +128,14 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   return L;
 }
 
-static int redo_smem_bytes(const PairConfig& cfg, int cap_redo, int ne_max) {
-  return std::max(make_layout(false, cap_redo, ne_max, cfg.warps, kRedoBig, cfg.pack).bytes,
-                  make_layout(false, cap_redo, ne_max, cfg.warps, kRedoFull, cfg.pack).bytes);
+static int redo_smem_bytes(const PairConfig& cfg, int cap_redo, int ne_max, int ext_max) {
+  return std::max(make_layout(false, cap_redo, ne_max, ext_max, cfg.warps, kRedoBig, cfg.pack).bytes,
+                  make_layout(false, cap_redo, ne_max, ext_max, cfg.warps, kRedoFull, cfg.pack).bytes);
 }
 
-int pair_smem_bytes(const PairConfig& cfg, int cap, int cap_redo, int ne_max) {
-  const int main = make_layout(cfg.fp64, cap, ne_max, cfg.warps, kMain, cfg.pack).bytes;
-  return cfg.fp64 ? main : std::max(main, redo_smem_bytes(cfg, cap_redo, ne_max));
+int pair_smem_bytes(const PairConfig& cfg, int cap, int cap_redo, int ne_max, int ext_max) {
+  const int main = make_layout(cfg.fp64, cap, ne_max, ext_max, cfg.warps, kMain, cfg.pack).bytes;
+  return cfg.fp64 ? main : std::max(main, redo_smem_bytes(cfg, cap_redo, ne_max, ext_max));
 }
 
 // Exact sum of FP32 terms in 64-bit fixed point (2^-32 resolution): the total
@@ -315,8 +317,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   const int EX = tx + 2, EY = ty + 2, EZ = tz + 2;
   const int NE = EX * EY * EZ;
   const int cap = MODE == kMain ? A.cap : A.cap_redo;
-  const Layout L = make_layout(FP64, cap, A.ne_max, nw, MODE, PACK);
-  int* lstart = (int*)(smem + L.lstart);
+  const Layout L = make_layout(FP64, cap, A.ne_max, A.ext_max, nw, MODE, PACK);
+  unsigned short* lstart = (unsigned short*)(smem + L.lstart);
   int* gfirst = (int*)(smem + L.gfirst);
   float* ox = (float*)(smem + L.ox);
   float* oy = (float*)(smem + L.oy);
@@ -324,7 +326,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   float* dyt = (float*)(smem + L.dyt);
   float* dzt = (float*)(smem + L.dzt);
   signed char* img = (signed char*)(smem + L.img);
-  double* red = (double*)(smem + L.red);
+  double* red = (double*)(smem + L.queue);  // scan and reduction scratch, before and after the queues' use
+  int* cw = (int*)(smem + L.cw);
   OwnLut* sown = (OwnLut*)(smem + L.lut);
   const signed char* srows = &sown->rows[0][0];
   float4* pf = (float4*)(smem + L.pf);
@@ -343,7 +346,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     int gc = B.cell0 + gx + B.nb[0] * (gy + B.nb[1] * gz);
     int s0 = A.cstart[gc];
     gfirst[e] = s0;
-    lstart[e] = A.cstart[gc + 1] - s0;
+    lstart[e] = (unsigned short)min(A.cstart[gc + 1] - s0, 0xffff);  // a larger count overflows any capacity
   }
   {
     const uint4* src = reinterpret_cast<const uint4*>(&c_own);
@@ -411,10 +414,13 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       lstart[k] = run;
       run += c;
     }
-    if (tid == blockDim.x - 1) lstart[NE] = run;
+    if (tid == blockDim.x - 1) {
+      lstart[NE] = (unsigned short)run;
+      cw[2] = run;
+    }
     __syncthreads();
   }
-  const int total = lstart[NE];
+  const int total = cw[2];
   if (!FP64 && MODE == kMain && total > cap) {  // the redo pass computes it at its capacity
     if (tid == 0) A.redo[atomicAdd(A.redo_n, 1)] = tile | kFullBit;
     return;
@@ -464,7 +470,6 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       code[t] = cc;
     }
   }
-  int* cw = (int*)(red + 8 * nw);
   int* big_flag = cw + 1;  // mixed form: a term was too large for the fixed-point sums
   if (tid == 0) {
     cw[0] = 0;  // work-unit counter
@@ -1086,8 +1091,8 @@ cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes) {
   return cudaFuncSetAttribute(pick_redo(cfg), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
 }
 
-int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max) {
-  const int smem = make_layout(cfg.fp64, cap, ne_max, cfg.warps, kMain, cfg.pack).bytes;
+int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max, int ext_max) {
+  const int smem = make_layout(cfg.fp64, cap, ne_max, ext_max, cfg.warps, kMain, cfg.pack).bytes;
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pick(cfg), 32 * cfg.warps, (size_t)smem) != cudaSuccess)
     return 0;
@@ -1099,12 +1104,12 @@ cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, in
   void* fn = pick(cfg);
   void* args[] = {(void*)&a};
   // smem_bytes (the larger of the two passes' needs) bounds both launches
-  const int main_smem = make_layout(cfg.fp64, a.cap, a.ne_max, cfg.warps, kMain, cfg.pack).bytes;
+  const int main_smem = make_layout(cfg.fp64, a.cap, a.ne_max, a.ext_max, cfg.warps, kMain, cfg.pack).bytes;
   if (main_smem > smem_bytes) return cudaErrorInvalidValue;
   cudaError_t e = cudaLaunchKernel(fn, dim3(ntiles), dim3(32 * cfg.warps), args, (size_t)main_smem, st);
   if (e != cudaSuccess || cfg.fp64) return e;
   // the redo pass: a few blocks per SM at most; nothing to do in a thermal system
-  const int redo_smem = redo_smem_bytes(cfg, a.cap_redo, a.ne_max);
+  const int redo_smem = redo_smem_bytes(cfg, a.cap_redo, a.ne_max, a.ext_max);
   if (redo_smem > smem_bytes) return cudaErrorInvalidValue;
   return cudaLaunchKernel(pick_redo(cfg), dim3(std::min(ntiles, kRedoBlocks)), dim3(32 * cfg.warps), args,
                           (size_t)redo_smem, st);

@@ -93,8 +93,8 @@ def test_first_pass_overflow_goes_to_the_redo_pass(gpulib):
             return s.counters()["max_tile_atoms"]
 
     occ_a = largest_tile(pos)
-    cap_first = (occ_a + occ_a // 16 + 32 + 31) // 32 * 32
-    cap_redo = (occ_a + occ_a // 4 + 64 + 31) // 32 * 32
+    cap_first = (occ_a + occ_a // 16 + 32 + 7) // 8 * 8
+    cap_redo = (occ_a + occ_a // 4 + 64 + 7) // 8 * 8
     posb = None
     for a in (0.25, 0.3, 0.35, 0.4, 0.45, 0.5):
         if cap_first < largest_tile(squeeze(a)) <= cap_redo:
@@ -109,5 +109,7 @@ def test_first_pass_overflow_goes_to_the_redo_pass(gpulib):
     err = np.sqrt(((f32 - f64) ** 2).sum(1))
     assert np.sqrt((err * err).mean()) / frms <= 1e-5
     # the largest errors: the closest pairs' r^-13 terms with an FP32 separation
-    assert err.max() / frms <= 1e-4
+    # (~1e-5 of forces up to ~1e4 at r ~ 0.65); a tile left out or counted
+    # twice would be off by the forces themselves
+    assert err.max() / np.sqrt((f64 * f64).sum(1)).max() <= 1e-4
     assert e32[0] == pytest.approx(e64, rel=1e-5)
