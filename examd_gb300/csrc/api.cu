@@ -451,6 +451,20 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     lj.minv[a] = 1.0 / m;
   }
 
+  // Tiles of a batch: the tile edge T is the densest box's.  A box with fewer
+  // atoms per cell gets tiles up to 2 cells longer per axis, as long as its
+  // expected staged atoms, (T + 2 + g)^3 per cell times its atoms per cell,
+  // stay within the densest box's (the largest tile sizes shared memory for
+  // the whole launch): fewer halo cells per home cell, the same footprint.
+  double dens_max = 0.0;
+  std::vector<double> dens(nboxes, 0.0);
+  for (int b = 0; b < nboxes; ++b) {
+    double cells = 1.0;
+    for (int a = 0; a < 3; ++a) cells *= std::max(1.0, std::floor(boxes[b].L[a] / bl));
+    dens[b] = (double)boxes[b].natoms / cells;
+    dens_max = std::max(dens_max, dens[b]);
+  }
+
   // boxes, cells, tiles
   std::vector<int4> tiles;
   std::vector<unsigned char> bmask;
@@ -491,12 +505,20 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     B.blif = (float)(1.0 / bl);
     B.cell0 = cell0;
     B.tile0 = (int)tiles.size() / 2;
+    int Tb[3] = {T[0], T[1], T[2]};
+    for (int g = 2; g > 0 && dens[b] > 0.0; --g) {
+      const double grown = (double)(T[0] + 2 + g) * (T[1] + 2 + g) * (T[2] + 2 + g) * dens[b];
+      if (grown <= (double)(T[0] + 2) * (T[1] + 2) * (T[2] + 2) * dens_max) {
+        for (int a = 0; a < 3; ++a) Tb[a] = T[a] + g;
+        break;
+      }
+    }
     int starts[3][1025];
     for (int a = 0; a < 3; ++a) {
-      // tiles of at most T cells (T or T - 1 when nb is not a multiple), so the
-      // largest staged tile, which sizes shared memory, stays (T + 2)^3 cells;
-      // every tile keeps >= 2 cells
-      B.nt[a] = std::max(1, std::min(B.nb[a] / 2, (B.nb[a] + T[a] - 1) / T[a]));
+      // tiles of at most Tb cells (Tb or Tb - 1 when nb is not a multiple), so
+      // the largest staged tile, which sizes shared memory, stays (Tb + 2)^3
+      // cells; every tile keeps >= 2 cells
+      B.nt[a] = std::max(1, std::min(B.nb[a] / 2, (B.nb[a] + Tb[a] - 1) / Tb[a]));
       for (int k = 0; k <= B.nt[a]; ++k) starts[a][k] = (int)((int64_t)k * B.nb[a] / B.nt[a]);
       for (int k = 0; k < B.nt[a]; ++k)
         if (starts[a][k + 1] - starts[a][k] + 2 > kMaxExt) {
