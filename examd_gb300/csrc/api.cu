@@ -162,7 +162,6 @@ struct examd_ctx {
   int* count = nullptr;
   int* cstart = nullptr;
   int* bsum = nullptr;
-  int* d_total = nullptr;
   void* Fown = nullptr;
   void* P = nullptr;
   double* tileE = nullptr;
@@ -230,7 +229,7 @@ void free_all(examd_ctx* ctx) {
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   ctx->gexec = nullptr;
   void* ptrs[] = {ctx->d_boxes, ctx->d_tiles, ctx->d_tile0, ctx->d_bmask, ctx->U, ctx->Uold, ctx->cellS,
-                  ctx->cellOld, ctx->slot, ctx->src, ctx->count, ctx->cstart, ctx->bsum, ctx->d_total,
+                  ctx->cellOld, ctx->slot, ctx->src, ctx->count, ctx->cstart, ctx->bsum,
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
                   ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor,
                   ctx->d_atom0, ctx->keAtom, ctx->partial, ctx->redo, ctx->redo_n};
@@ -624,7 +623,6 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   ALLOC(ctx->count, NC);
   ALLOC(ctx->cstart, NC + 1);
   ALLOC(ctx->bsum, 8192);
-  ALLOC(ctx->d_total, 1);
   if (ctx->pc.fp64) {
     double* f;
     ALLOC(f, 3 * N);
@@ -712,7 +710,6 @@ int finish_binning(examd_ctx* ctx, bool want_inv) {
   const int nsb = (nc + kScanTileHost - 1) / kScanTileHost;
   const int s = ctx->cur, d = 1 - ctx->cur;
   k_scan_reduce<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum);
-  k_scan_top<<<1, 1024, 0, st>>>(nsb, ctx->bsum, ctx->d_total);
   k_scan_final<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum, ctx->cstart);
   if (ctx->N > 0) {
     k_place<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, nc, ctx->cellOld, ctx->slot, ctx->cstart, ctx->src);

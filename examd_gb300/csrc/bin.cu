@@ -145,33 +145,18 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(int nc, const int*
   if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
-// One block scans up to kScanTile * 4 block sums.
-__global__ void __launch_bounds__(1024) k_scan_top(int nb, int* __restrict__ bsum, int* __restrict__ total_out) {
-  __shared__ int sh[32];
-  constexpr int kItems = 8;
-  int base = threadIdx.x * kItems;
-  int v[kItems], s = 0;
-#pragma unroll
-  for (int k = 0; k < kItems; ++k) {
-    v[k] = (base + k < nb) ? bsum[base + k] : 0;
-    s += v[k];
-  }
-  int total;
-  int ex = block_exclusive_scan(s, sh, total);
-#pragma unroll
-  for (int k = 0; k < kItems; ++k) {
-    if (base + k < nb) bsum[base + k] = ex;
-    ex += v[k];
-  }
-  if (threadIdx.x == 0) *total_out = total;
-}
-
 // Final pass: cstart = exclusive scan; counts are zeroed for the next binning.
+// Each block first sums the earlier blocks' sums itself (a few hundred to a
+// few thousand values), which saves a launch over a separate scan of them.
 // cstart[nc] (the atom count) is written by k_place.
 __global__ void __launch_bounds__(kScanThreads) k_scan_final(int nc, int* __restrict__ count,
                                                              const int* __restrict__ bsum,
                                                              int* __restrict__ cstart) {
   __shared__ int sh[kScanThreads / 32];
+  int pre = 0;
+  for (int k = threadIdx.x; k < (int)blockIdx.x; k += blockDim.x) pre += bsum[k];
+  int offset;
+  block_exclusive_scan(pre, sh, offset);  // offset: the block-wide sum
   int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   int v[kScanItems], s = 0;
 #pragma unroll
@@ -180,7 +165,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(int nc, int* __rest
     s += v[k];
   }
   int total;
-  int ex = block_exclusive_scan(s, sh, total) + bsum[blockIdx.x];
+  int ex = block_exclusive_scan(s, sh, total) + offset;
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     if (base + k < nc) {

@@ -164,6 +164,17 @@ __device__ __forceinline__ float d2f_rn_nonneg(double x) {
   return __uint_as_float(bits);
 }
 
+// float -> double, exact, by rebuilding the bit pattern on the integer pipe
+// (GB300 converts FP32 to FP64 on the FP64 pipe, at about 2 per clock per
+// SM).  Infinities and NaNs carry over; FP32 subnormals become signed zeros.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu, sign = b & 0x80000000u;
+  if (e == 0u) return __hiloint2double((int)sign, 0);
+  const unsigned ee = e == 0xffu ? 0x7ffu : e + (1023u - 127u);
+  return __hiloint2double((int)(sign | (ee << 20) | ((b & 0x7fffffu) >> 3)), (int)((b & 7u) << 29));
+}
+
 // n * 2^-k exactly, for 0 < n < 2^31 (0 for n = 0).
 __device__ __forceinline__ double mul_pow2(unsigned n, int k) {
   if (n == 0u) return 0.0;

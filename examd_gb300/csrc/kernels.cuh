@@ -17,7 +17,6 @@ __global__ void k_inverse(int64_t n, const int* id, int* inv);
 __global__ void k_bin(int64_t n, const double* X0, const double* X1, const double* X2, const int* meta,
                       const BoxDev* boxes, int* cellOld, int* slot, float4* Uold, int* count, int* status);
 __global__ void k_scan_reduce(int nc, const int* count, int* bsum);
-__global__ void k_scan_top(int nb, int* bsum, int* total_out);
 __global__ void k_scan_final(int nc, int* count, const int* bsum, int* cstart);
 __global__ void k_place(int64_t n, int nc, const int* cellOld, const int* slot, int* cstart, int* src);
 __global__ void k_finalize(int64_t n, const int* src, const int* cellOld, const int* cstart, const float4* Uold,

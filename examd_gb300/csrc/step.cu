@@ -51,9 +51,9 @@ __device__ __forceinline__ void gather_force(const StepArgs& a, int64_t s, doubl
     const float4* P = (const float4*)a.P;
     float4 v = Fo[s];
     if (m == 0) {
-      f[0] = v.x;
-      f[1] = v.y;
-      f[2] = v.z;
+      f[0] = f2d_exact(v.x);
+      f[1] = f2d_exact(v.y);
+      f[2] = f2d_exact(v.z);
       return;
     }
     KSum kx, ky, kz;
@@ -67,9 +67,9 @@ __device__ __forceinline__ void gather_force(const StepArgs& a, int64_t s, doubl
       ky.add(q.y);
       kz.add(q.z);
     }
-    f[0] = (double)(kx.s - kx.c);
-    f[1] = (double)(ky.s - ky.c);
-    f[2] = (double)(kz.s - kz.c);
+    f[0] = f2d_exact(kx.s - kx.c);
+    f[1] = f2d_exact(ky.s - ky.c);
+    f[2] = f2d_exact(kz.s - kz.c);
   }
 }
 
