@@ -167,6 +167,40 @@ def test_batched_boxes_equal_single(gpulib, oracle):
         off += len(p)
 
 
+def test_batched_uneven_density_both_forms(gpulib, oracle):
+    """Boxes of density 0.25 to 0.9 in one batch: the lighter boxes get longer
+    tiles (up to 2 cells per axis) than the densest one's.  Both forms
+    against the oracle per box, and the tile count below that of uniform
+    tiles."""
+    boxes, poss = [], []
+    for k, (n, rho) in enumerate(((4000, 0.9), (3000, 0.25), (2500, 0.5), (1200, 0.35))):
+        Lk = (n / rho) ** (1 / 3)
+        boxes.append([Lk, Lk, Lk])
+        poss.append(gpulib.gen_random(n, [Lk] * 3, 0.8, 200 + k))
+    allpos = np.concatenate(poss)
+    counts = [len(p) for p in poss]
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with gpulib.MidpointLJ(np.array(boxes), counts, precision=prec, tile=3) as s:
+            s.set_atoms(allpos)
+            out[prec] = s.forces(energy=True)[:2] + (s.counters()["tiles"],)
+    off = 0
+    for k, p in enumerate(poss):
+        ref = oracle.forces_typed(p, np.array(boxes[k]), 2.5)
+        mx, _ = rel_err(out["fp64"][0][off:off + len(p)], ref["forces"])
+        assert mx <= TOL64
+        assert out["fp64"][1][k] == pytest.approx(ref["epot"], rel=TOL64)
+        _, rms = rel_err(out["mixed"][0][off:off + len(p)], ref["forces"])
+        assert rms <= TOL_MIXED_RMS
+        off += len(p)
+    # uniform 3^3 tiles would need sum over boxes of ceil(nb / 3)^3 tiles
+    uniform = 0
+    for Lk in boxes:
+        nb = int(Lk[0] / 1.25)
+        uniform += max(1, min(nb // 2, -(-nb // 3))) ** 3
+    assert out["mixed"][2] < uniform
+
+
 def test_accumulate_and_forces_at(gpulib, oracle):
     L = np.array([15.0, 15.0, 16.0])
     pos = gas(gpulib, L, 1500, 0.8, 9)
