@@ -158,7 +158,6 @@ struct examd_ctx {
   int* cellS = nullptr;
   int* cellOld = nullptr;
   int* slot = nullptr;
-  int* src = nullptr;
   int* count = nullptr;
   int* cstart = nullptr;
   int* bsum = nullptr;
@@ -229,7 +228,7 @@ void free_all(examd_ctx* ctx) {
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   ctx->gexec = nullptr;
   void* ptrs[] = {ctx->d_boxes, ctx->d_tiles, ctx->d_tile0, ctx->d_bmask, ctx->U, ctx->Uold, ctx->cellS,
-                  ctx->cellOld, ctx->slot, ctx->src, ctx->count, ctx->cstart, ctx->bsum,
+                  ctx->cellOld, ctx->slot, ctx->count, ctx->cstart, ctx->bsum,
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
                   ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor,
                   ctx->d_atom0, ctx->keAtom, ctx->partial, ctx->redo, ctx->redo_n};
@@ -619,7 +618,6 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   ALLOC(ctx->cellS, N);
   ALLOC(ctx->cellOld, N);
   ALLOC(ctx->slot, N);
-  ALLOC(ctx->src, N);
   ALLOC(ctx->count, NC);
   ALLOC(ctx->cstart, NC + 1);
   ALLOC(ctx->bsum, 8192);
@@ -702,7 +700,7 @@ namespace {
 
 inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
 
-// Scan, place and final ordering after a counting pass; swaps the buffers.
+// Scan and final ordering after a counting pass; swaps the buffers.
 // want_inv: also record the caller -> sorted map (for the caller-order I/O).
 int finish_binning(examd_ctx* ctx, bool want_inv) {
   cudaStream_t st = ctx->st;
@@ -712,15 +710,12 @@ int finish_binning(examd_ctx* ctx, bool want_inv) {
   k_scan_reduce<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum);
   k_scan_final<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum, ctx->cstart);
   if (ctx->N > 0) {
-    k_place<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, nc, ctx->cellOld, ctx->slot, ctx->cstart, ctx->src);
-    k_finalize<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, ctx->src, ctx->cellOld, ctx->cstart, ctx->Uold,
+    k_finalize<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, ctx->cellOld, ctx->slot, ctx->cstart, ctx->Uold,
                                               ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->V[s][0],
                                               ctx->V[s][1], ctx->V[s][2], ctx->meta[s], ctx->id[s],
                                               ctx->X[d][0], ctx->X[d][1], ctx->X[d][2], ctx->V[d][0],
                                               ctx->V[d][1], ctx->V[d][2], ctx->meta[d], ctx->id[d], ctx->U,
                                               ctx->cellS, want_inv ? ctx->inv : nullptr);
-  } else {
-    k_place<<<1, 32, 0, st>>>(0, nc, ctx->cellOld, ctx->slot, ctx->cstart, ctx->src);
   }
   CK(cudaGetLastError());
   ctx->cur = d;

@@ -3,9 +3,13 @@
 //
 // Replaces exaMD_identify_block (SRC/exaMD_module.f90:101-125) and the
 // per-block linked lists built once by exaMD_particles_generate /
-// exaMD_read_particles (SRC/exaMD_input_formats.f90:66-92, 169-192).  The
-// result is the reference's own block order: cells in (z, y, x) order, atoms of
-// a cell in ascending caller index.  HBM-bound work.
+// exaMD_read_particles (SRC/exaMD_input_formats.f90:66-92, 169-192).  Cells
+// come in the reference's (z, y, x) block order; inside a cell the atoms keep
+// the order in which the counting pass drew their slots.  Neither form's
+// results depend on that order: the mixed form's force and energy sums are
+// exact fixed point and each pair's FP32 term is antisymmetric in its two
+// atoms, and the FP64 form's shared-memory atomics fix no order anyway.
+// HBM-bound work.
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -145,10 +149,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(int nc, const int*
   if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
-// Final pass: cstart = exclusive scan; counts are zeroed for the next binning.
-// Each block first sums the earlier blocks' sums itself (a few hundred to a
-// few thousand values), which saves a launch over a separate scan of them.
-// cstart[nc] (the atom count) is written by k_place.
+// Final pass: cstart = exclusive scan, cstart[nc] = the atom count; counts
+// are zeroed for the next binning.  Each block first sums the earlier blocks'
+// sums itself (a few hundred to a few thousand values), which saves a launch
+// over a separate scan of them.
 __global__ void __launch_bounds__(kScanThreads) k_scan_final(int nc, int* __restrict__ count,
                                                              const int* __restrict__ bsum,
                                                              int* __restrict__ cstart) {
@@ -166,6 +170,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(int nc, int* __rest
   }
   int total;
   int ex = block_exclusive_scan(s, sh, total) + offset;
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) cstart[nc] = offset + total;
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     if (base + k < nc) {
@@ -176,19 +181,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(int nc, int* __rest
   }
 }
 
-// Slot of every atom inside its cell (arbitrary order from the atomics).
-__global__ void k_place(int64_t n, int nc, const int* __restrict__ cellOld, const int* __restrict__ slot,
-                        int* __restrict__ cstart, int* __restrict__ src) {
-  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s == 0) cstart[nc] = (int)n;
-  if (s >= n) return;
-  src[cstart[cellOld[s]] + slot[s]] = (int)s;
-}
-
-// Final order: inside each cell the atoms are ranked by caller index (the
-// reference's linked-list order), then every per-atom array is gathered into
-// the other buffer.
-__global__ void k_finalize(int64_t n, const int* __restrict__ src, const int* __restrict__ cellOld,
+// Final order: every atom goes to its cell's range at the slot it drew in the
+// counting pass, and each per-atom array is scattered into the other buffer.
+__global__ void k_finalize(int64_t n, const int* __restrict__ cellOld, const int* __restrict__ slot,
                            const int* __restrict__ cstart, const float4* __restrict__ Uold,
                            const double* __restrict__ X0, const double* __restrict__ X1,
                            const double* __restrict__ X2, const double* __restrict__ V0,
@@ -198,15 +193,11 @@ __global__ void k_finalize(int64_t n, const int* __restrict__ src, const int* __
                            double* __restrict__ W1, double* __restrict__ W2, int* __restrict__ meta2,
                            int* __restrict__ id2, float4* __restrict__ U, int* __restrict__ cellS,
                            int* __restrict__ inv) {
-  int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  int s = src[j];
-  int c = cellOld[s];
-  int st = cstart[c], en = cstart[c + 1];
-  int myid = id[s];
-  int rank = 0;
-  for (int k = st; k < en; ++k) rank += (id[src[k]] < myid);
-  int d = st + rank;
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int c = cellOld[s];
+  const int d = cstart[c] + slot[s];
+  const int myid = id[s];
   Y0[d] = X0[s];
   Y1[d] = X1[s];
   Y2[d] = X2[s];

@@ -18,8 +18,7 @@ __global__ void k_bin(int64_t n, const double* X0, const double* X1, const doubl
                       const BoxDev* boxes, int* cellOld, int* slot, float4* Uold, int* count, int* status);
 __global__ void k_scan_reduce(int nc, const int* count, int* bsum);
 __global__ void k_scan_final(int nc, int* count, const int* bsum, int* cstart);
-__global__ void k_place(int64_t n, int nc, const int* cellOld, const int* slot, int* cstart, int* src);
-__global__ void k_finalize(int64_t n, const int* src, const int* cellOld, const int* cstart, const float4* Uold,
+__global__ void k_finalize(int64_t n, const int* cellOld, const int* slot, const int* cstart, const float4* Uold,
                            const double* X0, const double* X1, const double* X2, const double* V0,
                            const double* V1, const double* V2, const int* meta, const int* id, double* Y0,
                            double* Y1, double* Y2, double* W0, double* W1, double* W2, int* meta2, int* id2,
