@@ -154,7 +154,6 @@ struct examd_ctx {
   int* id[2] = {};
   int cur = 0;
   float4* U = nullptr;
-  float4* Uold = nullptr;
   int* cellS = nullptr;
   int* cellOld = nullptr;
   int* slot = nullptr;
@@ -227,7 +226,7 @@ int dalloc(examd_ctx* ctx, T** p, size_t count) {
 void free_all(examd_ctx* ctx) {
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   ctx->gexec = nullptr;
-  void* ptrs[] = {ctx->d_boxes, ctx->d_tiles, ctx->d_tile0, ctx->d_bmask, ctx->U, ctx->Uold, ctx->cellS,
+  void* ptrs[] = {ctx->d_boxes, ctx->d_tiles, ctx->d_tile0, ctx->d_bmask, ctx->U, ctx->cellS,
                   ctx->cellOld, ctx->slot, ctx->count, ctx->cstart, ctx->bsum,
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
                   ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor,
@@ -614,7 +613,6 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     ALLOC(ctx->id[b], N);
   }
   ALLOC(ctx->U, N);
-  ALLOC(ctx->Uold, N);
   ALLOC(ctx->cellS, N);
   ALLOC(ctx->cellOld, N);
   ALLOC(ctx->slot, N);
@@ -710,7 +708,7 @@ int finish_binning(examd_ctx* ctx, bool want_inv) {
   k_scan_reduce<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum);
   k_scan_final<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum, ctx->cstart);
   if (ctx->N > 0) {
-    k_finalize<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, ctx->cellOld, ctx->slot, ctx->cstart, ctx->Uold,
+    k_finalize<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, ctx->cellOld, ctx->slot, ctx->cstart, ctx->d_boxes,
                                               ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->V[s][0],
                                               ctx->V[s][1], ctx->V[s][2], ctx->meta[s], ctx->id[s],
                                               ctx->X[d][0], ctx->X[d][1], ctx->X[d][2], ctx->V[d][0],
@@ -938,7 +936,7 @@ int examd_gpu_set_atoms(examd_ctx* ctx, int64_t n, const double* pos, const int*
     k_load_bin<<<nblk(n), 256, 0, st>>>(n, ctx->stage, vel ? ctx->stage2 : nullptr, ctx->d_meta_in, ctx->d_boxes,
                                         ctx->p.strict_box, ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->V[s][0],
                                         ctx->V[s][1], ctx->V[s][2], ctx->meta[s], ctx->id[s], ctx->cellOld,
-                                        ctx->slot, ctx->Uold, ctx->count, ctx->status);
+                                        ctx->slot, ctx->count, ctx->status);
     CK(cudaGetLastError());
   }
   int rc = finish_binning(ctx, true);
@@ -984,7 +982,7 @@ int examd_gpu_forces_at(examd_ctx* ctx, const double* pos, double* forces, doubl
       CK(cudaStreamWaitEvent(st, ctx->ev_io[c], 0));
       k_gather_pos_bin_range<<<nblk(i1 - i0), 256, 0, st>>>(i0, i1, ctx->stage2, ctx->d_boxes, ctx->p.strict_box,
                                                             ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->meta[s],
-                                                            ctx->inv, ctx->cellOld, ctx->slot, ctx->Uold, ctx->count,
+                                                            ctx->inv, ctx->cellOld, ctx->slot, ctx->count,
                                                             ctx->status);
       CK(cudaGetLastError());
     }
@@ -1024,7 +1022,6 @@ KickArgs kick_args(examd_ctx* ctx, double ckick, double dt, bool drift, double h
   k.lj = ctx->lj;
   k.cellOld = ctx->cellOld;
   k.slot = ctx->slot;
-  k.Uold = ctx->Uold;
   k.count = ctx->count;
   k.status = ctx->status;
   return k;

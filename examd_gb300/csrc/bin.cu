@@ -17,20 +17,14 @@ namespace examd {
 
 __device__ __forceinline__ void bin_one(int s, double x, double y, double z, int meta,
                                         const BoxDev* __restrict__ boxes, int* __restrict__ cellOld,
-                                        int* __restrict__ slot, float4* __restrict__ Uold,
-                                        int* __restrict__ count, int* __restrict__ status) {
+                                        int* __restrict__ slot, int* __restrict__ count, int* __restrict__ status) {
   const BoxDev& B = boxes[meta >> 8];
   if (!(finite_bits(x) && finite_bits(y) && finite_bits(z))) {
     atomicOr(status, ST_NONFINITE);
     x = y = z = 0.0;
   }
-  float ux, uy, uz;
-  int cx = cell_offset(x, B, 0, ux);
-  int cy = cell_offset(y, B, 1, uy);
-  int cz = cell_offset(z, B, 2, uz);
-  int gc = B.cell0 + cx + B.nb[0] * (cy + B.nb[1] * cz);
+  const int gc = cell_of(x, y, z, B);
   cellOld[s] = gc;
-  Uold[s] = make_float4(ux, uy, uz, __int_as_float(meta & 0xff));
   slot[s] = atomicAdd(&count[gc], 1);
 }
 
@@ -41,8 +35,7 @@ __global__ void k_load_bin(int64_t n, const double* __restrict__ aos, const doub
                            double* __restrict__ X0, double* __restrict__ X1, double* __restrict__ X2,
                            double* __restrict__ V0, double* __restrict__ V1, double* __restrict__ V2,
                            int* __restrict__ meta, int* __restrict__ id, int* __restrict__ cellOld,
-                           int* __restrict__ slot, float4* __restrict__ Uold, int* __restrict__ count,
-                           int* __restrict__ status) {
+                           int* __restrict__ slot, int* __restrict__ count, int* __restrict__ status) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= n) return;
   int mt = meta_in[s];
@@ -66,7 +59,7 @@ __global__ void k_load_bin(int64_t n, const double* __restrict__ aos, const doub
   }
   meta[s] = mt;
   id[s] = (int)s;
-  bin_one((int)s, p[0], p[1], p[2], mt, boxes, cellOld, slot, Uold, count, status);
+  bin_one((int)s, p[0], p[1], p[2], mt, boxes, cellOld, slot, count, status);
 }
 
 // New positions for the caller's atoms [i0, i1) (AoS, caller order, as they
@@ -75,8 +68,8 @@ __global__ void k_gather_pos_bin_range(int64_t i0, int64_t i1, const double* __r
                                        const BoxDev* __restrict__ boxes, int strict, double* __restrict__ X0,
                                        double* __restrict__ X1, double* __restrict__ X2,
                                        const int* __restrict__ meta, const int* __restrict__ inv,
-                                       int* __restrict__ cellOld, int* __restrict__ slot, float4* __restrict__ Uold,
-                                       int* __restrict__ count, int* __restrict__ status) {
+                                       int* __restrict__ cellOld, int* __restrict__ slot, int* __restrict__ count,
+                                       int* __restrict__ status) {
   const int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= i1) return;
   const int s = inv[i];
@@ -92,21 +85,10 @@ __global__ void k_gather_pos_bin_range(int64_t i0, int64_t i1, const double* __r
   X0[s] = p[0];
   X1[s] = p[1];
   X2[s] = p[2];
-  bin_one(s, p[0], p[1], p[2], mt, boxes, cellOld, slot, Uold, count, status);
+  bin_one(s, p[0], p[1], p[2], mt, boxes, cellOld, slot, count, status);
 }
 
-// Bin the current positions without moving them (after a velocity-only change
-// or to rebuild the cell lists).
-__global__ void k_bin(int64_t n, const double* __restrict__ X0, const double* __restrict__ X1,
-                      const double* __restrict__ X2, const int* __restrict__ meta,
-                      const BoxDev* __restrict__ boxes, int* __restrict__ cellOld, int* __restrict__ slot,
-                      float4* __restrict__ Uold, int* __restrict__ count, int* __restrict__ status) {
-  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  bin_one((int)s, X0[s], X1[s], X2[s], meta[s], boxes, cellOld, slot, Uold, count, status);
-}
-
-// ---- exclusive scan of the cell counts (three passes) ----------------------
+// ---- exclusive scan of the cell counts (two passes) ------------------------
 constexpr int kScanThreads = 256, kScanItems = 8, kScanTile = kScanThreads * kScanItems;
 
 __device__ __forceinline__ int block_exclusive_scan(int v, int* sh, int& total) {
@@ -183,8 +165,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(int nc, int* __rest
 
 // Final order: every atom goes to its cell's range at the slot it drew in the
 // counting pass, and each per-atom array is scattered into the other buffer.
+// The pair kernel's FP32 cell offsets U are computed here from the FP64
+// position (the same exact rule as the cell), not carried from the counting
+// pass: 32 B less memory traffic per atom.
 __global__ void k_finalize(int64_t n, const int* __restrict__ cellOld, const int* __restrict__ slot,
-                           const int* __restrict__ cstart, const float4* __restrict__ Uold,
+                           const int* __restrict__ cstart, const BoxDev* __restrict__ boxes,
                            const double* __restrict__ X0, const double* __restrict__ X1,
                            const double* __restrict__ X2, const double* __restrict__ V0,
                            const double* __restrict__ V1, const double* __restrict__ V2,
@@ -197,16 +182,24 @@ __global__ void k_finalize(int64_t n, const int* __restrict__ cellOld, const int
   if (s >= n) return;
   const int c = cellOld[s];
   const int d = cstart[c] + slot[s];
-  const int myid = id[s];
-  Y0[d] = X0[s];
-  Y1[d] = X1[s];
-  Y2[d] = X2[s];
+  const int myid = id[s], mt = meta[s];
+  double x = X0[s], y = X1[s], z = X2[s];
+  Y0[d] = x;
+  Y1[d] = y;
+  Y2[d] = z;
   W0[d] = V0[s];
   W1[d] = V1[s];
   W2[d] = V2[s];
-  meta2[d] = meta[s];
+  meta2[d] = mt;
   id2[d] = myid;
-  U[d] = Uold[s];
+  if (!(finite_bits(x) && finite_bits(y) && finite_bits(z))) x = y = z = 0.0;  // as binned
+  const BoxDev& B = boxes[mt >> 8];
+  float4 u;
+  cell_offset(x, B, 0, u.x);
+  cell_offset(y, B, 1, u.y);
+  cell_offset(z, B, 2, u.z);
+  u.w = __int_as_float(mt & 0xff);
+  U[d] = u;
   cellS[d] = c;
   if (inv) inv[myid] = d;  // caller index -> sorted slot, when the caller's order is needed next
 }

@@ -204,6 +204,15 @@ __device__ __forceinline__ int cell_offset(double x, const BoxDev& B, int a, flo
   return c;
 }
 
+// Global cell of a position inside its box (the offsets are not needed).
+__device__ __forceinline__ int cell_of(double x, double y, double z, const BoxDev& B) {
+  float u;
+  const int cx = cell_offset(x, B, 0, u);
+  const int cy = cell_offset(y, B, 1, u);
+  const int cz = cell_offset(z, B, 2, u);
+  return B.cell0 + cx + B.nb[0] * (cy + B.nb[1] * cz);
+}
+
 // Periodic wrap of an FP64 coordinate into [0, L).  The in-range case is
 // decided on the bits; the rare out-of-range case is a separate function so
 // that its FP64 instructions are not executed speculatively by every thread.

@@ -8,17 +8,15 @@ namespace examd {
 // ---- bin.cu -----------------------------------------------------------------
 __global__ void k_load_bin(int64_t n, const double* aos, const double* vaos, const int* meta_in,
                            const BoxDev* boxes, int strict, double* X0, double* X1, double* X2, double* V0,
-                           double* V1, double* V2, int* meta, int* id, int* cellOld, int* slot, float4* Uold,
+                           double* V1, double* V2, int* meta, int* id, int* cellOld, int* slot,
                            int* count, int* status);
 __global__ void k_gather_pos_bin_range(int64_t i0, int64_t i1, const double* aos, const BoxDev* boxes, int strict,
                                        double* X0, double* X1, double* X2, const int* meta, const int* inv,
-                                       int* cellOld, int* slot, float4* Uold, int* count, int* status);
+                                       int* cellOld, int* slot, int* count, int* status);
 __global__ void k_inverse(int64_t n, const int* id, int* inv);
-__global__ void k_bin(int64_t n, const double* X0, const double* X1, const double* X2, const int* meta,
-                      const BoxDev* boxes, int* cellOld, int* slot, float4* Uold, int* count, int* status);
 __global__ void k_scan_reduce(int nc, const int* count, int* bsum);
 __global__ void k_scan_final(int nc, int* count, const int* bsum, int* cstart);
-__global__ void k_finalize(int64_t n, const int* cellOld, const int* slot, const int* cstart, const float4* Uold,
+__global__ void k_finalize(int64_t n, const int* cellOld, const int* slot, const int* cstart, const BoxDev* boxes,
                            const double* X0, const double* X1, const double* X2, const double* V0,
                            const double* V1, const double* V2, const int* meta, const int* id, double* Y0,
                            double* Y1, double* Y2, double* W0, double* W1, double* W2, int* meta2, int* id2,
@@ -115,7 +113,6 @@ struct KickArgs {
   // binning outputs (drift only)
   int* cellOld;
   int* slot;
-  float4* Uold;
   int* count;
   int* status;
 };

@@ -14,17 +14,12 @@
 
 namespace examd {
 
-__device__ __forceinline__ void bin_store(int s, double x, double y, double z, int meta, const BoxDev& B,
+__device__ __forceinline__ void bin_store(int s, double x, double y, double z, const BoxDev& B,
                                           int* __restrict__ cellOld, int* __restrict__ slot,
-                                          float4* __restrict__ Uold, int* __restrict__ count) {
+                                          int* __restrict__ count) {
   // same rule as bin.cu: exact cell of the FP64 position on the grid c * bl
-  float ux, uy, uz;
-  int cx = cell_offset(x, B, 0, ux);
-  int cy = cell_offset(y, B, 1, uy);
-  int cz = cell_offset(z, B, 2, uz);
-  int gc = B.cell0 + cx + B.nb[0] * (cy + B.nb[1] * cz);
+  const int gc = cell_of(x, y, z, B);
   cellOld[s] = gc;
-  Uold[s] = make_float4(ux, uy, uz, __int_as_float(meta & 0xff));
   slot[s] = atomicAdd(&count[gc], 1);
 }
 
@@ -244,7 +239,7 @@ __global__ void k_kick(const KickArgs k) {
       atomicOr(k.status, ST_NONFINITE);
       x[0] = x[1] = x[2] = 0.0;
     }
-    bin_store((int)s, x[0], x[1], x[2], mt, B, k.cellOld, k.slot, k.Uold, k.count);
+    bin_store((int)s, x[0], x[1], x[2], B, k.cellOld, k.slot, k.count);
   }
 }
 
