@@ -392,8 +392,8 @@ def main():
                        "parallelism": f"replicas{ws}"},
             "clocks": clk.summary(),
             "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n},
-            # per step: kick+drift+bin, 2 scan kernels, place, finalize, pair, redo pass
-            "gpu_launches": 7 * args.steps + 1,
+            # per step: kick+drift+bin count, 2 scan kernels, finalize, pair, redo pass
+            "gpu_launches": 6 * args.steps + 1,
             # pair rates of the timed run (the counters of one force evaluation x steps / time)
             "pairs": {"interactions_per_s": cnt["accepted"] * args.steps * ws / (t_ms * 1e-3),
                       "candidates_per_s": cnt["candidates"] * args.steps * ws / (t_ms * 1e-3),
