@@ -187,15 +187,22 @@ class MidpointLJ:
         return f, ep, w
 
     def forces_at(self, pos, out=None, accumulate=False, energy=False):
-        """New positions (same atoms, caller order) and one force evaluation."""
+        """New positions (same atoms, caller order) and one force evaluation.
+
+        With pos and out in pinned memory (pinned_empty) the library replays the
+        call as a captured CUDA graph from the second call with the same arrays;
+        the energies then land in pinned arrays of this object and are copied."""
         p = pos if (isinstance(pos, np.ndarray) and pos.dtype == np.float64 and pos.flags.c_contiguous) \
             else np.ascontiguousarray(pos, dtype=np.float64)
         f = out if out is not None else np.zeros((self.n, 3))
-        ep = np.zeros(self.nboxes) if energy else None
-        w = np.zeros(self.nboxes) if energy else None
+        ep = w = None
+        if energy:
+            if getattr(self, "_pinned_ew", None) is None:
+                self._pinned_ew = (pinned_empty((self.nboxes,)), pinned_empty((self.nboxes,)))
+            ep, w = self._pinned_ew
         self._chk(self._lib.examd_gpu_forces_at(self._ctx, _d(p), _d(f), _d(ep), _d(w), 1 if accumulate else 0),
                   "examd_gpu_forces_at")
-        return f, ep, w
+        return f, (ep.copy() if energy else None), (w.copy() if energy else None)
 
     def run(self, nsteps, dt, graph_chunk=0, energies=False):
         """Velocity-Verlet steps.  Returns dict(ms, ekin[steps, boxes], epot[steps, boxes])."""

@@ -196,6 +196,15 @@ struct examd_ctx {
   cudaGraphExec_t gexec = nullptr;
   int g_parity = -1, g_chunk = 0, g_energy = -1, g_cap = 0;
   double g_dt = 0.0;
+  // the force call at new positions (examd_gpu_forces_at) as a CUDA graph,
+  // one per parity of the sort's double buffer, for a caller that passes the
+  // same pinned buffers every time (an MD driver's arrays)
+  struct IoGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void *pos = nullptr, *forces = nullptr, *epot = nullptr, *virial = nullptr;
+    int accumulate = -1, cap = 0, cap_redo = 0;
+    bool pack = false;
+  } io_graph[2];
 
   int cuda_fail(cudaError_t e, const char* what) {
     lasterr = std::string(what) + ": " + cudaGetErrorString(e);
@@ -226,6 +235,8 @@ int dalloc(examd_ctx* ctx, T** p, size_t count) {
 void free_all(examd_ctx* ctx) {
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   ctx->gexec = nullptr;
+  for (auto& g : ctx->io_graph)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
   void* ptrs[] = {ctx->d_boxes, ctx->d_tiles, ctx->d_tile0, ctx->d_bmask, ctx->U, ctx->cellS,
                   ctx->cellOld, ctx->slot, ctx->count, ctx->cstart, ctx->bsum,
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
@@ -867,7 +878,9 @@ StepArgs step_args(examd_ctx* ctx) {
 // chunks of its own order: the device->host copy of chunk c (second stream)
 // overlaps the gather of chunk c + 1.  With accumulate, the caller's forces
 // come in on the second stream while the pair kernel runs.
-int forces_common(examd_ctx* ctx, double* forces, double* epot, double* virial, int accumulate) {
+// The work of the force call, queued on the context's streams; the second
+// stream rejoins the first at the end (so the sequence can be captured).
+int enqueue_forces(examd_ctx* ctx, double* forces, double* epot, double* virial, int accumulate) {
   cudaStream_t st = ctx->st, st2 = ctx->st2;
   const bool energy = epot || virial;
   const int64_t N = ctx->N;
@@ -901,13 +914,34 @@ int forces_common(examd_ctx* ctx, double* forces, double* epot, double* virial, 
   }
   if (epot) CK(cudaMemcpyAsync(epot, ctx->boxE, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (virial) CK(cudaMemcpyAsync(virial, ctx->boxW, ctx->nboxes * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaEventRecord(ctx->ev_io[3 * kIoChunks], st2));
+  CK(cudaStreamWaitEvent(st, ctx->ev_io[3 * kIoChunks], 0));
+  return EXAMD_OK;
+}
+
+// Waits for the force call and reads its status word.
+int finish_forces(examd_ctx* ctx) {
   CK(queue_status(ctx));
-  CK(cudaStreamSynchronize(st2));
-  CK(cudaStreamSynchronize(st));
-  rc = take_status(ctx);
+  CK(cudaStreamSynchronize(ctx->st));
+  const int rc = take_status(ctx);
   if (rc) return rc;
   ctx->forces_valid = true;
   return EXAMD_OK;
+}
+
+int forces_common(examd_ctx* ctx, double* forces, double* epot, double* virial, int accumulate) {
+  const int rc = enqueue_forces(ctx, forces, epot, virial, accumulate);
+  return rc ? rc : finish_forces(ctx);
+}
+
+bool pinned(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
 }
 
 }  // namespace
@@ -958,11 +992,13 @@ int examd_gpu_forces(examd_ctx* ctx, double* forces, double* epot, double* viria
   return forces_common(ctx, forces, epot, virial, accumulate);
 }
 
-int examd_gpu_forces_at(examd_ctx* ctx, const double* pos, double* forces, double* epot, double* virial,
-                        int accumulate) {
-  if (!ctx || (ctx->N > 0 && !pos)) return EXAMD_ERR_ARG;
-  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
-  cudaSetDevice(ctx->dev);
+}  // extern "C"
+
+namespace {
+
+// The force call at new positions, queued (see examd_gpu_forces_at).
+int enqueue_forces_at(examd_ctx* ctx, const double* pos, double* forces, double* epot, double* virial,
+                      int accumulate) {
   cudaStream_t st = ctx->st, st2 = ctx->st2;
   const int s = ctx->cur;
   const int64_t N = ctx->N;
@@ -989,7 +1025,62 @@ int examd_gpu_forces_at(examd_ctx* ctx, const double* pos, double* forces, doubl
   }
   int rc = finish_binning(ctx, true);
   if (rc) return rc;
-  return forces_common(ctx, forces, epot, virial, accumulate);
+  return enqueue_forces(ctx, forces, epot, virial, accumulate);
+}
+
+int finish_forces_at_eager(examd_ctx* ctx, const double* pos, double* forces, double* epot, double* virial,
+                           int accumulate) {
+  const int rc = enqueue_forces_at(ctx, pos, forces, epot, virial, accumulate);
+  return rc ? rc : finish_forces(ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
+int examd_gpu_forces_at(examd_ctx* ctx, const double* pos, double* forces, double* epot, double* virial,
+                        int accumulate) {
+  if (!ctx || (ctx->N > 0 && !pos)) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  CK(ensure_inv(ctx));  // outside any captured sequence
+  if (ctx->N < kIoMinChunk || !pinned(pos) || !pinned(forces) || !pinned(epot) || !pinned(virial))
+    return finish_forces_at_eager(ctx, pos, forces, epot, virial, accumulate);
+  // same pinned buffers as last time at this parity: replay the captured call
+  auto& g = ctx->io_graph[ctx->cur];
+  const bool hit = g.exec && g.pos == pos && g.forces == forces && g.epot == epot && g.virial == virial &&
+                   g.accumulate == accumulate && g.cap == ctx->cap && g.cap_redo == ctx->cap_redo &&
+                   g.pack == ctx->pc.pack;
+  if (!hit) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = examd_ctx::IoGraph{};
+    const int parity = ctx->cur;
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_forces_at(ctx, pos, forces, epot, virial, accumulate);
+    cudaError_t ce = cudaStreamEndCapture(ctx->st, &graph);
+    ctx->cur = parity;  // capture only recorded the work
+    if (rc) return rc;
+    if (ce != cudaSuccess) return ctx->cuda_fail(ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+      g.exec = nullptr;
+      return ctx->cuda_fail(ce, "cudaGraphInstantiate");
+    }
+    g.pos = pos;
+    g.forces = forces;
+    g.epot = epot;
+    g.virial = virial;
+    g.accumulate = accumulate;
+    g.cap = ctx->cap;
+    g.cap_redo = ctx->cap_redo;
+    g.pack = ctx->pc.pack;
+  }
+  CK(cudaGraphLaunch(g.exec, ctx->st));
+  ctx->cur = 1 - ctx->cur;  // the host-side effects of the captured call
+  ctx->inv_valid = true;
+  return finish_forces(ctx);
 }
 
 }  // extern "C"
