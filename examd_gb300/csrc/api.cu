@@ -449,6 +449,26 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     lj.p32[k].rc2 = (float)(r * r);
     lj.p32[k].rcut2 = (float)rcut2;
     lj.p32[k].eshift = (float)eshift;
+    {
+      // |F(r)| = 24 eps (2 s^12 - s^6) / r, s = sigma / r, falls monotonically
+      // from r -> 0 to its zero at 2^(1/6) sigma: bisect for |F| = kFixMaxForce,
+      // then widen by 1e-4 (the FP32 d2 of a pair and the FP32 force differ
+      // from the exact ones by far less)
+      auto fmag = [&](double rr) {
+        const double s6 = std::pow(s / rr, 6.0);
+        return 24.0 * e * (2.0 * s6 * s6 - s6) / rr;
+      };
+      double lo = 1e-3 * s, hi = std::pow(2.0, 1.0 / 6.0) * s;
+      if (!(fmag(lo) > kFixMaxForce)) {
+        hi = lo;
+      } else {
+        for (int it = 0; it < 200; ++it) {
+          const double mid = 0.5 * (lo + hi);
+          (fmag(mid) > kFixMaxForce ? lo : hi) = mid;
+        }
+      }
+      lj.p32[k].r2big = (float)(hi * hi * (1.0 + 1e-4));
+    }
     rc2max = std::max(rc2max, lj.p32[k].rc2);
   }
   lj.rc2max = rc2max;

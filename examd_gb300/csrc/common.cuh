@@ -53,7 +53,14 @@ struct BoxDev {
 struct LJ32 {
   float sig2, m24eps, c4eps, rc2;  // m24eps = -24 eps (dg prefactor)
   float rcut2, eshift;
+  float r2big;  // r^2 below which |F| >= kFixMaxForce (mixed form: left to the redo pass)
 };
+
+// Mixed form: pair-force magnitude at which a term leaves the fixed-point sums
+// (2^15 scale, int32) for the redo pass (r < ~0.74 sigma at eps = 1); every
+// component of a kept term is below 2^26 in fixed point, so a component's
+// int32 sum needs more than 32 near-maximal terms of one sign to overflow.
+constexpr float kFixMaxForce = 2048.f;
 struct LJ64 {
   double sig2, eps24, eps4, rc2;   // as user_func.f90:58-59 computes them
   double rcut2, eshift;

@@ -28,11 +28,11 @@
 // Accumulation.  Mixed form: each per-atom force component is an exact 32-bit
 // fixed-point sum in shared memory (scale 2^15, native integer atomics), so
 // the result does not depend on the order of the terms and is reproducible
-// bit for bit.  A term of magnitude >= 1024 (r < 0.79 sigma at eps = 1) is
-// left out and flags the tile, so every fixed-point term is below 2^25 and a
-// component's sum could leave the int32 range only through more than 64
-// near-maximal terms of one sign on one atom, i.e. 64 neighbours within about
-// 0.8 sigma on one side, which no physical configuration has.  A second
+// bit for bit.  A term of magnitude >= 2048 (r < 0.74 sigma at eps = 1) is
+// left out and flags the tile, so every fixed-point term is below 2^26 and a
+// component's sum could leave the int32 range only through more than 32
+// near-maximal terms of one sign on one atom, i.e. 32 neighbours within about
+// 0.75 sigma on one side, which no physical configuration has.  A second
 // launch (k_pair_redo) recomputes the flagged tiles, sums their large terms
 // in FP32 and adds them to the outputs; thermal configurations flag no tile
 // and the launch returns at once (only the rare FP32 sums' order can vary
@@ -60,7 +60,6 @@ constexpr int kQueue = 64;    // per-warp queue of accepted pairs
 constexpr int kParts = 2;     // work units per 32 staged atoms (1, 3 and 4 measured slower)
 constexpr float kFix = 32768.f;        // fixed-point scale 2^15
 constexpr float kFixInv = 1.f / 32768.f;
-constexpr float kFixMax = 1024.f;      // larger terms are left to the redo pass
 constexpr int kRedoBlocks = 152;       // grid of the redo pass (1 per SM)
 // Passes of the mixed form's tile body: the first pass; the redo pass's two
 // kinds of tile, one whose large terms were left out (only those are summed
@@ -164,11 +163,11 @@ struct FixSum {
 // the same i (a segmented shuffle scan; integer sums, so the result is exact)
 // and each segment's last lane adds its total: one shared atomic per segment
 // instead of one per pair on the same address.
-// A pair-force term too large for the fixed-point sums (a component of
-// magnitude >= kFixMax, i.e. r < ~0.79 sigma at eps = 1, which thermal
-// configurations do not reach) is left out here and raises the tile's flag
-// (*big_flag); the redo pass adds it.  SIDE (the full redo pass): such terms
-// go to the FP32 side sums fr instead.
+// A pair-force term too large for the fixed-point sums (|F| >= kFixMaxForce,
+// decided on r^2 < r2big of the type pair: r < ~0.74 sigma at eps = 1, which
+// thermal configurations do not reach) is left out here and raises the
+// tile's flag (*big_flag); the redo pass adds it.  SIDE (the full redo pass):
+// such terms go to the FP32 side sums fr instead.
 template <bool MULTI, bool ENERGY, bool COUNT, bool SIDE>
 __device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, const int* qk, int* fa, float* fr,
                                             int cap, const PairArgs& A, FixSum& ek, FixSum& wk, int& nacc,
@@ -179,6 +178,7 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, c
   const bool act = lane < cnt;
   int i = -1, m = 0;
   float fx = 0.f, fy = 0.f, fz = 0.f;
+  bool big = false;
   if (act) {
     const int slot = (qh + lane) & (kQueue - 1);
     const float4 d = qd[slot];
@@ -187,6 +187,7 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, c
     m = (key >> 14) & 0x3fff;
     LJ32 P = lj.p32[0];
     if (MULTI) P = lj.p32[((key >> 28) & 3) * lj.nt + (key >> 30)];
+    big = d.w < P.r2big;  // left to the redo pass
     float dg = 0.f, e = 0.f;
     const int rv = pair_fn32<ENERGY>(lj.pot, d.w, P, dg, e);
     if (rv == 0) {
@@ -203,8 +204,6 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, c
       atomicOr(A.status, ST_PAIRFN);
     }
   }
-  // terms too large for the fixed-point sums: left to the redo pass
-  const bool big = act && fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) >= kFixMax * kFix;
   int ix = 0, iy = 0, iz = 0;
   if (act && !big) {
     ix = __float2int_rn(fx);
@@ -533,7 +532,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     if (pair_fn32<false>(A.lj.pot, dq.w, P, dg, e) != 0) return;
     const float dgs = kFix * dg;
     const float fx = dgs * dq.x, fy = dgs * dq.y, fz = dgs * dq.z;
-    if (!(fmaxf(fabsf(fx), fmaxf(fabsf(fy), fabsf(fz))) >= kFixMax * kFix)) return;
+    if (!(dq.w < P.r2big)) return;
     atomicAdd(&fr[i], fx * kFixInv);
     atomicAdd(&fr[cap + i], fy * kFixInv);
     atomicAdd(&fr[2 * cap + i], fz * kFixInv);

@@ -17,7 +17,8 @@ def forces(gpulib, pos, L, precision):
 
 def test_close_pairs_match_fp64(gpulib):
     """40 atoms moved to 0.62-0.75 sigma from another atom of an FCC liquid:
-    pair forces of 1.6e3-1.1e4 epsilon/sigma, all outside the fixed-point range."""
+    pair forces of 1.6e3-1.1e4 epsilon/sigma, most of them above the
+    fixed-point range (2048)."""
     from examd_gb300 import workloads as W
     c = W.liquid_fcc(8)  # 2048 atoms
     L = np.asarray(c["boxes"][0], dtype=np.float64)
