@@ -3,9 +3,10 @@
 //
 // The reference has no counterpart: its work decomposition is the METIS
 // partition of the block graph (SRC/exaMD_partitioning.f90), fixed by the
-// process count.  Here the unit of work is a CTA tile of home cells; its edge
-// (3-6 cells) trades halo overhead against shared memory per CTA and CTAs per
-// SM, and the warps per CTA trade latency hiding against tail imbalance.  The
+// process count.  Here the unit of work is a CTA tile of home cells; its
+// shape (cubes of 3-6 cells, and cubes stretched by one cell on one or two
+// axes) trades halo overhead against shared memory per CTA and CTAs per SM,
+// and the warps per CTA trade latency hiding against tail imbalance.  The
 // cell edge stays at the reference's rc/2: a larger edge only adds candidate
 // pairs, and a smaller one breaks the 63-entry table.
 //
@@ -92,14 +93,15 @@ extern "C" int examd_autotune(const examd_params* params, int nboxes, const exam
     if (best_ms) *best_ms = ms;
     return EXAMD_OK;
   }
-  const int edges[] = {3, 4, 5, 6};
+  const int shapes[][3] = {{3, 3, 3}, {4, 3, 3}, {4, 4, 3}, {4, 4, 4}, {5, 4, 4}, {5, 5, 4},
+                           {5, 5, 5}, {6, 5, 5}, {6, 6, 5}, {6, 6, 6}};
   const int widths[] = {8, 4};
   double best_t = INFINITY;
   int last_rc = EXAMD_ERR_CELL_OVERFLOW;
-  for (int e : edges)
+  for (const auto& sh : shapes)
     for (int w : widths) {
       examd_params p = *params;
-      p.tile[0] = p.tile[1] = p.tile[2] = e;
+      for (int a = 0; a < 3; ++a) p.tile[a] = sh[a];
       p.warps = w;
       examd_ctx* ctx = nullptr;
       int rc = examd_gpu_create(&p, nboxes, boxes, &ctx);

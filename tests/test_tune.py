@@ -1,4 +1,4 @@
-"""examd_autotune: the tile edge and CTA width picked by timing, with a text cache."""
+"""examd_autotune: the tile shape and CTA width picked by timing, with a text cache."""
 import ctypes as C
 
 import numpy as np
@@ -25,7 +25,8 @@ def test_tuned_choice_cached_and_equivalent(gpulib, tmp_path, precision, tol):
     pos = gpulib.gen_random(6000, L, 0.85, 21)
     cache = tmp_path / "tune.txt"
     r = gpulib.autotune(L, [len(pos)], pos, cache=cache, precision=precision, rc=2.5)
-    assert r["tile"][0] in (3, 4, 5, 6) and r["tile"] == (r["tile"][0],) * 3
+    t = sorted(r["tile"])
+    assert t[0] in (3, 4, 5, 6) and t[2] - t[0] <= 1
     assert r["warps"] in (4, 8) and r["ms"] > 0
     assert len(cache.read_text().splitlines()) == 1
     r2 = gpulib.autotune(L, [len(pos)], pos, cache=cache, precision=precision, rc=2.5)
