@@ -4,8 +4,8 @@
 // The reference has no counterpart: its work decomposition is the METIS
 // partition of the block graph (SRC/exaMD_partitioning.f90), fixed by the
 // process count.  Here the unit of work is a CTA tile of home cells; its
-// shape (cubes of 3-6 cells, and cubes stretched by one cell on one or two
-// axes) trades halo overhead against shared memory per CTA and CTAs per SM,
+// shape (cubes of 3-6 cells, cubes stretched by one cell on one or two axes,
+// and a few stretched by two along x) trades halo overhead against shared memory per CTA and CTAs per SM,
 // and the warps per CTA trade latency hiding against tail imbalance.  The
 // cell edge stays at the reference's rc/2: a larger edge only adds candidate
 // pairs, and a smaller one breaks the 63-entry table.
@@ -93,8 +93,8 @@ extern "C" int examd_autotune(const examd_params* params, int nboxes, const exam
     if (best_ms) *best_ms = ms;
     return EXAMD_OK;
   }
-  const int shapes[][3] = {{3, 3, 3}, {4, 3, 3}, {4, 4, 3}, {4, 4, 4}, {5, 4, 4}, {5, 5, 4},
-                           {5, 5, 5}, {6, 5, 5}, {6, 6, 5}, {6, 6, 6}};
+  const int shapes[][3] = {{3, 3, 3}, {4, 3, 3}, {4, 4, 3}, {4, 4, 4}, {5, 4, 4}, {6, 4, 4}, {5, 5, 4},
+                           {6, 5, 4}, {5, 5, 5}, {6, 5, 5}, {6, 6, 5}, {6, 6, 6}};
   const int widths[] = {8, 4};
   double best_t = INFINITY;
   int last_rc = EXAMD_ERR_CELL_OVERFLOW;
