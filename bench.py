@@ -295,15 +295,15 @@ def main():
     sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **lj)
     sysm.set_atoms(case["pos"], case["types"], case["vel"])
     equilibrate(sysm, case["natoms"], temps, eq_steps, eq_every, dt)
-    tuning = {"tile": "default", "warps": "default"}
+    tuning = {"tile": "default", "warps": "default", "tile_balance": 0}
     if not args.no_tune:
-        # tile edge and warps per CTA for the equilibrated atoms (examd_autotune)
+        # tile shape, warps per CTA and tile split for the equilibrated atoms (examd_autotune)
         pos_eq, vel_eq = sysm.state()
         tuning = ex.autotune(case["boxes"], case["natoms"], pos_eq, case["types"], precision="mixed", device=lr,
                              **lj)
         sysm.close()
         sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, tile=tuning["tile"],
-                             warps=tuning["warps"], **lj)
+                             warps=tuning["warps"], tile_balance=tuning["tile_balance"], **lj)
         sysm.set_atoms(pos_eq, case["types"], vel_eq)
     chunk = max(2, args.chunk // 2 * 2)
     wsteps = max(args.warmup, chunk + 2)
@@ -386,7 +386,7 @@ def main():
             "config": {"workload": label, "atoms": n, "boxes": nboxes, "rc": lj.get("rc"), "dt": dt,
                        "precision": "mixed", "graph_chunk": chunk,
                        "tile": list(tuning["tile"]) if isinstance(tuning["tile"], tuple) else tuning["tile"],
-                       "warps": tuning["warps"],
+                       "warps": tuning["warps"], "tile_balance": tuning["tile_balance"],
                        "l2": "working set > L2 (per-step HBM traffic ~0.2 KB per atom)" if n * 200 > 129e6
                        else "working set fits L2 (small configuration)",
                        "parallelism": f"replicas{ws}"},

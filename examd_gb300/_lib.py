@@ -49,6 +49,7 @@ class Params(C.Structure):
         ("device", C.c_int),
         ("potential", C.c_int),
         ("pair_tables", C.c_int),
+        ("tile_balance", C.c_int),
     ]
 
 

@@ -47,7 +47,8 @@ PAIR_TABLES = {"auto": 0, "wide": 1, "compact": 2}
 
 
 def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None, block_length=None,
-           tile=None, warps=None, strict_box=False, device=0, potential="lj", pair_tables="auto"):
+           tile=None, warps=None, strict_box=False, device=0, potential="lj", pair_tables="auto",
+           tile_balance=0):
     """examd_params and the examd_box array of a system, from Python arguments."""
     lib = _L.load()
     b = np.atleast_2d(np.asarray(boxes, dtype=np.float64))
@@ -81,6 +82,9 @@ def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, 
     if pair_tables not in PAIR_TABLES:
         raise ValueError(f"pair_tables must be one of {sorted(PAIR_TABLES)}")
     p.pair_tables = PAIR_TABLES[pair_tables]
+    if tile_balance not in (0, 1):
+        raise ValueError("tile_balance must be 0 (split by cell count) or 1 (by width)")
+    p.tile_balance = int(tile_balance)
     arr = (_L.Box * b.shape[0])()
     for k in range(b.shape[0]):
         for a in range(3):
@@ -90,9 +94,10 @@ def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, 
 
 
 def autotune(boxes, natoms, pos, types=None, cache=None, **kw):
-    """Tile edge and warps per CTA for this system, picked by timing the pair
-    kernel on these atoms (examd_autotune).  cache: path of a text cache of
-    earlier choices, or None.  Returns dict(tile, warps, ms per launch)."""
+    """Tile shape, warps per CTA and tile split for this system, picked by
+    timing the pair kernel on these atoms (examd_autotune).  cache: path of a
+    text cache of earlier choices, or None.  Returns dict(tile, warps,
+    tile_balance, ms per launch)."""
     lib, p, arr, b, n, _ = _setup(boxes, natoms, **kw)
     pp = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
     t = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
@@ -101,7 +106,8 @@ def autotune(boxes, natoms, pos, types=None, cache=None, **kw):
     path = None if cache is None else os.fsencode(cache)
     check(lib.examd_autotune(C.byref(p), len(n), arr, len(pp), _d(pp), _i(t), path, C.byref(best), C.byref(ms)),
           "examd_autotune")
-    return {"tile": tuple(int(v) for v in best.tile), "warps": int(best.warps), "ms": ms.value}
+    return {"tile": tuple(int(v) for v in best.tile), "warps": int(best.warps),
+            "tile_balance": int(best.tile_balance), "ms": ms.value}
 
 
 class MidpointLJ:
@@ -114,13 +120,15 @@ class MidpointLJ:
     reference (exaMD.f90:56).  potential: the pair function, "lj" (the
     reference's lennardjones_12), "lj_shifted" or "wca".  pair_tables: the
     mixed form's per-warp tables, "auto" (compact where that fits more CTAs
-    on an SM), "wide" or "compact"; the forces are the same bit for bit."""
+    on an SM), "wide" or "compact"; the forces are the same bit for bit.
+    tile_balance: 0 splits each axis into tiles by cell count, 1 by width (the
+    wide last cell that absorbs the box's remainder counts as two)."""
 
     def __init__(self, boxes, natoms, *, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None,
                  block_length=None, tile=None, warps=None, strict_box=False, device=0, potential="lj",
-                 pair_tables="auto"):
+                 pair_tables="auto", tile_balance=0):
         lib, p, arr, b, n, m = _setup(boxes, natoms, precision, eps, sigma, rc, ntypes, mass, block_length, tile,
-                                      warps, strict_box, device, potential, pair_tables)
+                                      warps, strict_box, device, potential, pair_tables, tile_balance)
         self._lib = lib
         self.nboxes = int(b.shape[0])
         self.natoms = n.copy()
@@ -138,9 +146,9 @@ class MidpointLJ:
 
     @classmethod
     def tuned(cls, boxes, natoms, pos, types=None, vel=None, cache=None, **kw):
-        """A system whose tile shape and CTA width the autotuner picked for these atoms."""
+        """A system whose tile shape, CTA width and tile split the autotuner picked for these atoms."""
         r = autotune(boxes, natoms, pos, types, cache, **kw)
-        kw = dict(kw, tile=r["tile"], warps=r["warps"])
+        kw = dict(kw, tile=r["tile"], warps=r["warps"], tile_balance=r["tile_balance"])
         s = cls(boxes, natoms, **kw)
         s.set_atoms(pos, types, vel)
         s.tuning = r

@@ -146,6 +146,7 @@ struct examd_ctx {
   // device buffers
   BoxDev* d_boxes = nullptr;
   int4* d_tiles = nullptr;
+  int* d_order = nullptr;  // pair-kernel launch order of the tiles
   int* d_tile0 = nullptr;
   unsigned char* d_bmask = nullptr;
   double* X[2][3] = {};
@@ -237,7 +238,7 @@ void free_all(examd_ctx* ctx) {
   ctx->gexec = nullptr;
   for (auto& g : ctx->io_graph)
     if (g.exec) cudaGraphExecDestroy(g.exec);
-  void* ptrs[] = {ctx->d_boxes, ctx->d_tiles, ctx->d_tile0, ctx->d_bmask, ctx->U, ctx->cellS,
+  void* ptrs[] = {ctx->d_boxes, ctx->d_tiles, ctx->d_order, ctx->d_tile0, ctx->d_bmask, ctx->U, ctx->cellS,
                   ctx->cellOld, ctx->slot, ctx->count, ctx->cstart, ctx->bsum,
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
                   ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor,
@@ -398,7 +399,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   ctx->pc.multi = nt > 1;
   ctx->pc.pack = p.pair_tables == 2;
   ctx->pair_tables = p.pair_tables;
-  if (p.pair_tables < 0 || p.pair_tables > 2) {
+  if (p.pair_tables < 0 || p.pair_tables > 2 || p.tile_balance < 0 || p.tile_balance > 1) {
     delete ctx;
     return EXAMD_ERR_ARG;
   }
@@ -545,9 +546,16 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     for (int a = 0; a < 3; ++a) {
       // tiles of at most Tb cells (Tb or Tb - 1 when nb is not a multiple), so
       // the largest staged tile, which sizes shared memory, stays (Tb + 2)^3
-      // cells; every tile keeps >= 2 cells
-      B.nt[a] = std::max(1, std::min(B.nb[a] / 2, (B.nb[a] + Tb[a] - 1) / Tb[a]));
-      for (int k = 0; k <= B.nt[a]; ++k) starts[a][k] = (int)((int64_t)k * B.nb[a] / B.nt[a]);
+      // cells; every tile keeps >= 2 cells.  tile_balance = 1: a last cell at
+      // least 1.5 edges wide counts as two cells (nv = nb + 1 in the split),
+      // so the tile that holds it has one cell fewer
+      const double wide = (B.L[a] - (B.nb[a] - 1) * bl) / bl;  // the last cell's width in edges
+      const int nv = B.nb[a] + (p.tile_balance == 1 && wide >= 1.5 ? 1 : 0);
+      B.nt[a] = std::max(1, std::min(B.nb[a] / 2, (nv + Tb[a] - 1) / Tb[a]));
+      for (int k = 0; k < B.nt[a]; ++k) starts[a][k] = (int)((int64_t)k * nv / B.nt[a]);
+      starts[a][B.nt[a]] = B.nb[a];
+      if (B.nt[a] > 1 && starts[a][B.nt[a]] - starts[a][B.nt[a] - 1] < 2)  // keep >= 2 cells: even split
+        for (int k = 0; k <= B.nt[a]; ++k) starts[a][k] = (int)((int64_t)k * B.nb[a] / B.nt[a]);
       for (int k = 0; k < B.nt[a]; ++k)
         if (starts[a][k + 1] - starts[a][k] + 2 > kMaxExt) {
           delete ctx;
@@ -594,6 +602,37 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     delete ctx;
     return EXAMD_ERR_ARG;
   }
+  // Launch order of the pair kernel: the tiles by estimated cost, costliest
+  // first, so that the grid ends on its cheapest CTAs (longest processing
+  // time first; the per-tile outputs keep the tile's index).  The estimate is
+  // the tile's staged atoms plus twice its home atoms times the atoms per cell
+  // (its pair work), from cell volumes: the last cell of an axis is wider.
+  std::vector<int> order(ctx->ntiles);
+  {
+    std::vector<double> cost(ctx->ntiles);
+    for (int t = 0; t < ctx->ntiles; ++t) {
+      const int4 d0 = tiles[2 * t], d1 = tiles[2 * t + 1];
+      const BoxDev& B = ctx->bh[d0.x];
+      const int org[3] = {d0.y, d0.z, d0.w}, len[3] = {d1.x, d1.y, d1.z};
+      double vh = 1.0, ve = 1.0;
+      for (int a = 0; a < 3; ++a) {
+        const double wide = (B.L[a] - (B.nb[a] - 1) * B.bl) / B.bl;  // the last cell's width in cell edges
+        double h = 0.0, e = 0.0;
+        for (int c = org[a] - 1; c <= org[a] + len[a]; ++c) {
+          const int g = (c + B.nb[a]) % B.nb[a];
+          const double w = g == B.nb[a] - 1 ? wide : 1.0;
+          e += w;
+          if (c >= org[a] && c < org[a] + len[a]) h += w;
+        }
+        vh *= h;
+        ve *= e;
+      }
+      const double n = (double)boxes[d0.x].natoms * B.bl * B.bl * B.bl / (B.L[0] * B.L[1] * B.L[2]);
+      cost[t] = n * (ve + 2.0 * vh * n);
+    }
+    for (int t = 0; t < ctx->ntiles; ++t) order[t] = t;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  }
 
   OwnLut lut;
   if (!build_own_lut(lut)) {
@@ -633,6 +672,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   const size_t N = (size_t)ctx->N, NC = (size_t)ctx->NC;
   ALLOC(ctx->d_boxes, nboxes);
   ALLOC(ctx->d_tiles, tiles.size());
+  ALLOC(ctx->d_order, ctx->ntiles);
   ALLOC(ctx->d_tile0, nboxes + 1);
   ALLOC(ctx->d_bmask, NC);
   for (int b = 0; b < 2; ++b) {
@@ -695,6 +735,8 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   bool ok = cudaMemcpyAsync(ctx->d_boxes, ctx->bh.data(), nboxes * sizeof(BoxDev), cudaMemcpyHostToDevice, st) ==
                 cudaSuccess &&
             cudaMemcpyAsync(ctx->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, st) ==
+                cudaSuccess &&
+            cudaMemcpyAsync(ctx->d_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st) ==
                 cudaSuccess &&
             cudaMemcpyAsync(ctx->d_tile0, ctx->tile0.data(), (nboxes + 1) * sizeof(int), cudaMemcpyHostToDevice,
                             st) == cudaSuccess &&
@@ -846,6 +888,7 @@ int update_capacity(examd_ctx* ctx) {
 PairArgs pair_args(examd_ctx* ctx) {
   PairArgs a{};
   a.tiles = ctx->d_tiles;
+  a.order = ctx->d_order;
   a.boxes = ctx->d_boxes;
   a.cstart = ctx->cstart;
   a.U = ctx->U;

@@ -26,6 +26,7 @@ constexpr int kScanTileHost = 2048;  // cells per scan block (kScanThreads * kSc
 // ---- pair.cu ----------------------------------------------------------------
 struct PairArgs {
   const int4* tiles;  // 2 int4 per tile
+  const int* order;   // launch order: CTA b computes tile order[b] (the costliest tiles first)
   const BoxDev* boxes;
   const int* cstart;
   const float4* U;

@@ -108,7 +108,7 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.cw = o;     o = align16(o + 16);  // unit counter, large-term flag, staged-atom total
   L.r2l = o;    o = align16(o + (fp64 ? 64 * nw : 0));  // rank -> lane tables (FP64 form)
   L.lut = o;    o = align16(o + (int)sizeof(OwnLut));
-  const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64 : 20 * kQueue + (pack ? kWarpTabCompact : kWarpTabWide)) * nw;
+  const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64 : 16 * kQueue + (pack ? kWarpTabCompact : kWarpTabWide)) * nw;
   L.queue = o;  o = align16(o + qbytes);
   L.pf = o;     o = align16(o + 16 * cap);
   if (fp64) {
@@ -120,7 +120,7 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   }
   L.code = o;   o = align16(o + 2 * cap);
   L.fr = L.queue;
-  if (!fp64 && (mode == kRedoFull || (mode == kRedoBig && 3 * 4 * cap > 20 * kQueue * nw))) {
+  if (!fp64 && (mode == kRedoFull || (mode == kRedoBig && 3 * 4 * cap > 16 * kQueue * nw))) {
     L.fr = o;   o = align16(o + 3 * 4 * cap);
   }
   L.bytes = o;
@@ -156,7 +156,8 @@ struct FixSum {
 };
 
 // Forces of cnt queued accepted pairs, one per lane: entry = (d = x_j - x_i,
-// r^2) and key = i | j << 14 | type_i << 28 | type_j << 30.  user_func.f90:58-69
+// key) with key = i | j << 14 | type_i << 28 | type_j << 30; r^2 is recomputed
+// with the distance test's expression, so it has the same bits.  user_func.f90:58-69
 // in FP32: dg = -24 eps (2 s^12 - s^6) / r^2, f_i += dg d, f_j -= dg d.
 // The queue keeps an atom's accepted pairs next to each other, so the i-side
 // fixed-point terms are first summed over segments of each run of lanes with
@@ -181,8 +182,9 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, c
   bool big = false;
   if (act) {
     const int slot = (qh + lane) & (kQueue - 1);
-    const float4 d = qd[slot];
-    const unsigned key = (unsigned)qk[slot];
+    float4 d = qd[slot];
+    const unsigned key = __float_as_uint(d.w);
+    d.w = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));  // r^2 exactly as the distance test computed it
     i = key & 0x3fff;
     m = (key >> 14) & 0x3fff;
     LJ32 P = lj.p32[0];
@@ -481,15 +483,15 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   double esum = 0.0, wsum = 0.0;  // FP64 form
   FixSum ek, wk;                  // mixed form: exact fixed-point sums of FP32 terms
   int ncand = 0, neval = 0, nacc = 0;
-  // per-warp queue of accepted pairs
-  // (mixed: separation and r^2, plus the key; FP64 form: the key only)
-  constexpr int kQd = FP64 ? 0 : 16;
+  // per-warp queue of accepted pairs (mixed form: the separation and the key
+  // in one 16-byte entry, r^2 recomputed from it; FP64 form: the key only)
+  constexpr int kQe = FP64 ? 4 : 16;  // bytes per queue entry
   float4* qd = (float4*)(smem + L.queue) + warp * kQueue;
-  int* qk = (int*)(smem + L.queue + kQd * kQueue * nw) + warp * kQueue;
+  int* qk = (int*)(smem + L.queue) + warp * kQueue;
   // per-warp tables (kWarpTab*): one step's items (ptA, ptB) and, mixed
   // form, the work unit's atoms (bt)
   unsigned char* wtab =
-      smem + L.queue + (kQd + 4) * kQueue * nw + warp * (FP64 ? kWarpTabFp64 : (PACK ? kWarpTabCompact : kWarpTabWide));
+      smem + L.queue + kQe * kQueue * nw + warp * (FP64 ? kWarpTabFp64 : (PACK ? kWarpTabCompact : kWarpTabWide));
   float4* ptA = (float4*)wtab;
   void* ptB = wtab + 32 * 16;
   float4* btA = (float4*)(wtab + (PACK ? 32 * 24 : 32 * 32));
@@ -504,8 +506,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     const unsigned bal = __ballot_sync(FULL, acc);
     if (acc) {
       const int p = (qh + qn + __popc(bal & lt)) & (kQueue - 1);
-      if (!FP64) qd[p] = dq;
-      qk[p] = key;
+      if (FP64)
+        qk[p] = key;
+      else
+        qd[p] = make_float4(dq.x, dq.y, dq.z, __int_as_float(key));
     }
     qn += __popc(bal);
     if (qn >= 32) {  // a batch only moves the ring's head
@@ -794,9 +798,12 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
               }
           }
           // distance from the atom to the row's cell boxes
-          const float gy = dy > 0 ? oy[ly + dy] - py : (dy < 0 ? py - oy[ly + dy + 1] : 0.f);
-          const float gz = dz > 0 ? oz[lz + dz] - pz : (dz < 0 ? pz - oz[lz + dz + 1] : 0.f);
-          const float g2 = fmaxf(gy, 0.f) * fmaxf(gy, 0.f) + fmaxf(gz, 0.f) * fmaxf(gz, 0.f);
+          // (one table load per axis: the row's near face is ext coordinate
+          // l + d for d > 0 and l + d + 1 for d < 0)
+          const float ty = oy[ly + dy + (dy < 0)] - py, tz = oz[lz + dz + (dz < 0)] - pz;
+          const float gy = dy == 0 ? 0.f : fmaxf(dy > 0 ? ty : -ty, 0.f);
+          const float gz = dz == 0 ? 0.f : fmaxf(dz > 0 ? tz : -tz, 0.f);
+          const float g2 = gy * gy + gz * gz;
           const float tr = prune2 - g2;
           if (tr < 0.f) mask = 0;
           mask &= ~((xm2 > tr ? 1 : 0) | (xm1 > tr ? 2 : 0) | (xp1 > tr ? 8 : 0) | (xp2 > tr ? 16 : 0));
@@ -1019,7 +1026,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
 
 template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, bool PACK>
 __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
-  pair_tile<FP64, MULTI, ENERGY, COUNT, kMain, PACK>(A, blockIdx.x);
+  pair_tile<FP64, MULTI, ENERGY, COUNT, kMain, PACK>(A, A.order[blockIdx.x]);
 }
 
 // Mixed form: the redo pass over the tiles that k_pair listed (normally none,

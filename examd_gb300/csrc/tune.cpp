@@ -6,7 +6,12 @@
 // process count.  Here the unit of work is a CTA tile of home cells; its
 // shape (cubes of 3-6 cells, cubes stretched by one cell on one or two axes,
 // and a few stretched by two along x) trades halo overhead against shared memory per CTA and CTAs per SM,
-// and the warps per CTA trade latency hiding against tail imbalance.  The
+// and the warps per CTA trade latency hiding against tail imbalance.  Where
+// a box's last cell on some axis is at least about 1.5 edges wide (it
+// absorbs the box's remainder), each shape is also tried with the tiles split
+// by width (examd_params.tile_balance = 1): the tile that holds that cell has
+// one cell fewer, which shrinks the largest tile and so the shared memory of
+// every CTA, at the price of a few more tiles.  The
 // cell edge stays at the reference's rc/2: a larger edge only adds candidate
 // pairs, and a smaller one breaks the 63-entry table.
 //
@@ -39,14 +44,14 @@ std::string cache_key(const examd_params& p, int nboxes, const examd_box* boxes,
   for (int b = 0; b < nboxes; ++b) vol += boxes[b].L[0] * boxes[b].L[1] * boxes[b].L[2];
   for (int k = 0; k < p.ntypes * p.ntypes; ++k) rcmax = std::fmax(rcmax, p.rc[k]);
   char buf[256];
-  // atom count in quarter-octaves, density to 0.05
-  std::snprintf(buf, sizeof buf, "%s|%s|nt%d|rc%.4g|boxes%d|n%.2f|rho%.2f", dev.c_str(),
+  // atom count in quarter-octaves, density to 0.05; "tb": choices that include the tile split
+  std::snprintf(buf, sizeof buf, "%s|%s|nt%d|rc%.4g|boxes%d|n%.2f|rho%.2f|tb", dev.c_str(),
                 p.precision == EXAMD_FP64 ? "fp64" : "mixed", p.ntypes, rcmax, nboxes,
                 std::round(std::log2((double)(n > 0 ? n : 1)) * 4.0) / 4.0, std::round(n / vol * 20.0) / 20.0);
   return buf;
 }
 
-bool cache_lookup(const char* path, const std::string& key, int tile[3], int* warps, double* ms) {
+bool cache_lookup(const char* path, const std::string& key, int tile[3], int* warps, int* balance, double* ms) {
   if (!path) return false;
   std::FILE* f = std::fopen(path, "r");
   if (!f) return false;
@@ -55,13 +60,14 @@ bool cache_lookup(const char* path, const std::string& key, int tile[3], int* wa
   while (std::fgets(line, sizeof line, f)) {
     char* sep = std::strrchr(line, '|');
     if (!sep || (size_t)(sep - line) != key.size() || std::strncmp(line, key.c_str(), key.size()) != 0) continue;
-    int t0, t1, t2, w;
+    int t0, t1, t2, w, tb;
     double m;
-    if (std::sscanf(sep + 1, "%d %d %d %d %lf", &t0, &t1, &t2, &w, &m) == 5) {
+    if (std::sscanf(sep + 1, "%d %d %d %d %lf %d", &t0, &t1, &t2, &w, &m, &tb) == 6 && (tb == 0 || tb == 1)) {
       tile[0] = t0;
       tile[1] = t1;
       tile[2] = t2;
       *warps = w;
+      *balance = tb;
       *ms = m;
       hit = true;  // the last entry wins
     }
@@ -71,12 +77,28 @@ bool cache_lookup(const char* path, const std::string& key, int tile[3], int* wa
 }
 
 // The key's fields are joined by '|'; the choice follows the last '|'.
-void cache_store(const char* path, const std::string& key, const int tile[3], int warps, double ms) {
+void cache_store(const char* path, const std::string& key, const int tile[3], int warps, int balance, double ms) {
   if (!path) return;
   std::FILE* f = std::fopen(path, "a");
   if (!f) return;
-  std::fprintf(f, "%s|%d %d %d %d %.17g\n", key.c_str(), tile[0], tile[1], tile[2], warps, ms);
+  std::fprintf(f, "%s|%d %d %d %d %.17g %d\n", key.c_str(), tile[0], tile[1], tile[2], warps, ms, balance);
   std::fclose(f);
+}
+
+// Whether some box has a last cell of about 1.5 edges or more on some axis
+// (the cell edge before its rounding to 14 significant bits, which moves it
+// by less than 1e-4 of itself; the margin covers that).
+bool has_wide_cell(const examd_params& p, int nboxes, const examd_box* boxes) {
+  double rcmax = 0.0;
+  for (int k = 0; k < p.ntypes * p.ntypes; ++k) rcmax = std::fmax(rcmax, p.rc[k]);
+  const double bl = p.cell_edge > 0 ? p.cell_edge : 0.5 * rcmax;
+  if (!(bl > 0)) return false;
+  for (int b = 0; b < nboxes; ++b)
+    for (int a = 0; a < 3; ++a) {
+      const double q = boxes[b].L[a] / bl;
+      if (q - std::floor(q) >= 0.45) return true;
+    }
+  return false;
 }
 
 }  // namespace
@@ -88,7 +110,7 @@ extern "C" int examd_autotune(const examd_params* params, int nboxes, const exam
   const std::string key = cache_key(*params, nboxes, boxes, n);
   examd_params out = *params;
   double ms = 0.0;
-  if (cache_lookup(cache_path, key, out.tile, &out.warps, &ms)) {
+  if (cache_lookup(cache_path, key, out.tile, &out.warps, &out.tile_balance, &ms)) {
     *best = out;
     if (best_ms) *best_ms = ms;
     return EXAMD_OK;
@@ -96,31 +118,34 @@ extern "C" int examd_autotune(const examd_params* params, int nboxes, const exam
   const int shapes[][3] = {{3, 3, 3}, {4, 3, 3}, {4, 4, 3}, {4, 4, 4}, {5, 4, 4}, {6, 4, 4}, {5, 5, 4},
                            {6, 5, 4}, {5, 5, 5}, {6, 5, 5}, {6, 6, 5}, {6, 6, 6}};
   const int widths[] = {8, 4};
+  const int nbal = has_wide_cell(*params, nboxes, boxes) ? 2 : 1;
   double best_t = INFINITY;
   int last_rc = EXAMD_ERR_CELL_OVERFLOW;
-  for (const auto& sh : shapes)
-    for (int w : widths) {
-      examd_params p = *params;
-      for (int a = 0; a < 3; ++a) p.tile[a] = sh[a];
-      p.warps = w;
-      examd_ctx* ctx = nullptr;
-      int rc = examd_gpu_create(&p, nboxes, boxes, &ctx);
-      double t = 0.0;
-      if (rc == EXAMD_OK) rc = examd_gpu_set_atoms(ctx, n, pos, type, nullptr);
-      if (rc == EXAMD_OK) rc = examd_gpu_time_forces(ctx, kReps, nullptr, &t);
-      if (ctx) examd_gpu_destroy(ctx);
-      if (rc == EXAMD_ERR_NO_DEVICE || rc == EXAMD_ERR_ARG || rc == EXAMD_ERR_OUTSIDE) return rc;
-      if (rc != EXAMD_OK) {
-        last_rc = rc;
-        continue;
+  for (int tb = 0; tb < nbal; ++tb)
+    for (const auto& sh : shapes)
+      for (int w : widths) {
+        examd_params p = *params;
+        for (int a = 0; a < 3; ++a) p.tile[a] = sh[a];
+        p.warps = w;
+        p.tile_balance = tb;
+        examd_ctx* ctx = nullptr;
+        int rc = examd_gpu_create(&p, nboxes, boxes, &ctx);
+        double t = 0.0;
+        if (rc == EXAMD_OK) rc = examd_gpu_set_atoms(ctx, n, pos, type, nullptr);
+        if (rc == EXAMD_OK) rc = examd_gpu_time_forces(ctx, kReps, nullptr, &t);
+        if (ctx) examd_gpu_destroy(ctx);
+        if (rc == EXAMD_ERR_NO_DEVICE || rc == EXAMD_ERR_ARG || rc == EXAMD_ERR_OUTSIDE) return rc;
+        if (rc != EXAMD_OK) {
+          last_rc = rc;
+          continue;
+        }
+        if (t < best_t) {
+          best_t = t;
+          out = p;
+        }
       }
-      if (t < best_t) {
-        best_t = t;
-        out = p;
-      }
-    }
   if (!std::isfinite(best_t)) return last_rc;
-  cache_store(cache_path, key, out.tile, out.warps, best_t);
+  cache_store(cache_path, key, out.tile, out.warps, out.tile_balance, best_t);
   *best = out;
   if (best_ms) *best_ms = best_t;
   return EXAMD_OK;

@@ -88,6 +88,11 @@ typedef struct examd_params {
   int potential;      /* EXAMD_POT_*                                          */
   int pair_tables;    /* mixed form's per-warp tables in the pair kernel:     */
                       /* 0 = chosen by occupancy, 1 = wide, 2 = compact       */
+  int tile_balance;   /* split of an axis into tiles: 0 = by cell count;      */
+                      /* 1 = by width, where the last cell (which absorbs the */
+                      /* box's remainder) is >= 1.5 edges wide it counts as   */
+                      /* two, so its tile has one cell fewer and the largest  */
+                      /* tile, which sizes shared memory, is smaller          */
 } examd_params;
 
 /* One independent periodic box of a batched ensemble. */
@@ -181,9 +186,11 @@ int examd_kinetic_static(int device, int64_t natoms, int nboxes,
 int examd_gpu_scale_velocities(examd_ctx *ctx, const double *factor);
 
 /* Autotuner (no counterpart in the reference, whose decomposition is the
- * METIS partition): time the pair kernel on these atoms for tile edges of 3-6
- * home cells and 4 or 8 warps per CTA, and return the fastest in *best (a copy
- * of *params with tile and warps set) and its time per launch in *best_ms.
+ * METIS partition): time the pair kernel on these atoms for tile shapes of 3-6
+ * home cells per axis, 4 or 8 warps per CTA and, where a box has a last cell
+ * of about 1.5 edges or more, both tile splits (tile_balance), and return the
+ * fastest in *best (a copy of *params with tile, warps and tile_balance set)
+ * and its time per launch in *best_ms.
  * cache_path (may be NULL): a text file of earlier choices keyed by device,
  * precision, types, cutoff, box count, atom count and density; a hit returns
  * without timing, a miss is appended.  pos/type as in examd_gpu_set_atoms. */

@@ -4,6 +4,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -86,3 +87,32 @@ def test_no_device_is_reported(gpulib):
     box[0].natoms = 10
     ctx = C.c_void_p()
     assert L.examd_gpu_create(C.byref(p), 1, box, C.byref(ctx)) == _lib.ERR_NO_DEVICE
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of examd_params, examd_box and examd_stats have the
+    C structs' sizes and field offsets (compiled from the header with gcc)."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    from examd_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"examd_params": _lib.Params, "examd_box": _lib.Box, "examd_stats": _lib.Stats}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "examd_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'  printf("{cname}.{f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(ln.split() for ln in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                       check=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(got[cname]) == C.sizeof(py), cname
+        for f in py._fields_:
+            assert int(got[f"{cname}.{f[0]}"]) == getattr(py, f[0]).offset, f"{cname}.{f[0]}"
