@@ -124,12 +124,17 @@ def main(argv=None):
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--evals", type=int, default=3)
     ap.add_argument("--steps", type=int, default=0, help="then this many velocity-Verlet steps (dt 0.005)")
-    ap.add_argument("--tile", type=int, default=None)
+    ap.add_argument("--tile", type=int, nargs="+", default=None, help="tile edge, or edges per axis")
+    ap.add_argument("--tile-balance", type=int, default=0, choices=[0, 1],
+                    help="split of each axis into tiles: 0 by cell count, 1 by width")
     a = ap.parse_args(argv)
     kw = {"liquid": {"nc": a.nc}, "slab": {"n": a.n}, "ensemble": {"nboxes": a.nboxes},
           "binary_mixture": {"m": a.m}}[a.case]
     case = CASES[a.case](**kw)
-    with system(case, a.precision, tile=a.tile) as s:
+    tile = None if a.tile is None else (a.tile * 3 if len(a.tile) == 1 else a.tile)
+    if tile is not None and len(tile) != 3:
+        ap.error("--tile takes one edge or three")
+    with system(case, a.precision, tile=tile, tile_balance=a.tile_balance) as s:
         for _ in range(a.evals):
             s.forces()
         cnt = s.counters()
