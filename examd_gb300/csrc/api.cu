@@ -92,8 +92,10 @@ bool build_own_lut(OwnLut& L) {
             if (class_ok(cx, h[0]) && class_ok(cy, h[1]) && class_ok(cz, h[2])) mask |= 1u << (kv.first + 2);
           }
           if (r == kRows - 1 && class_ok(cx, 0) && class_ok(cy, 0) && class_ok(cz, 0)) mask |= 1u << 2;
-          L.lut[cls][r] = (unsigned char)mask;
-          if (mask) L.rlist[cls][L.nrow[cls]++] = (unsigned char)r;
+          if (mask) {
+            L.lut[cls][L.nrow[cls]] = (unsigned char)mask;  // by position in the class's row list
+            L.rlist[cls][L.nrow[cls]++] = (unsigned char)r;
+          }
         }
       }
   return true;
@@ -344,7 +346,9 @@ int examd_own_table(signed char* rows, unsigned char* lut) {
   OwnLut L;
   if (!build_own_lut(L)) return EXAMD_ERR_ARG;
   std::memcpy(rows, L.rows, sizeof(L.rows));
-  std::memcpy(lut, L.lut, sizeof(L.lut));
+  std::memset(lut, 0, sizeof(L.lut));  // by row, as the header documents it
+  for (int c = 0; c < kClasses; ++c)
+    for (int n = 0; n < L.nrow[c]; ++n) lut[c * kRows + L.rlist[c][n]] = L.lut[c][n];
   return EXAMD_OK;
 }
 

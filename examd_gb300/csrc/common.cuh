@@ -79,12 +79,14 @@ struct LJTable {
 
 // Ownership masks of the midpoint table, filled once per process.
 //   c_rows[r] = (dy, dz) of row r (r = 12: the self row (0,0))
-//   c_lut[cls][r] = 5-bit mask over dx = -2..2 of the cell pairs (A, A+d)
-//   owned by the tile when A's position class is cls.  Row 12 uses bit 2 for
-//   the pairs inside A (a1 < a2) and bits 3, 4 for dx = +1, +2.
+//   lut[cls][n] = 5-bit mask over dx = -2..2 of the cell pairs (A, A+d) of
+//   row rlist[cls][n] owned by the tile when A's position class is cls (by
+//   position in the class's row list, so that a kernel reads the row and its
+//   mask side by side).  Row 12 uses bit 2 for the pairs inside A (a1 < a2)
+//   and bits 3, 4 for dx = +1, +2.
 // 16-byte aligned so that a CTA copies it to shared memory as uint4 words.
 struct __align__(16) OwnLut {
-  unsigned char lut[kClasses][kRows];     // dx mask per position class and row
+  unsigned char lut[kClasses][kRows];     // dx mask per position class and row-list position
   signed char rows[kRows][2];             // (dy, dz) of row r
   unsigned char nrow[kClasses];           // rows with a nonzero mask
   unsigned char rlist[kClasses][kRows];   // those rows, ascending

@@ -102,8 +102,8 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.ox = o;     o = align16(o + 4 * (ext_max + 1));
   L.oy = o;     o = align16(o + 4 * (ext_max + 1));
   L.oz = o;     o = align16(o + 4 * (ext_max + 1));
-  L.dyt = o;    o = align16(o + 4 * ext_max * kDT);
-  L.dzt = o;    o = align16(o + 4 * ext_max * kDT);
+  L.dyt = o;    o = align16(o + 8 * ext_max * kDT);
+  L.dzt = o;    o = align16(o + 8 * ext_max * kDT);
   L.img = o;    o = align16(o + (fp64 ? 3 * 32 : 0));  // periodic image per ext coordinate (FP64 form)
   L.cw = o;     o = align16(o + 16);  // unit counter, large-term flag, staged-atom total
   L.r2l = o;    o = align16(o + (fp64 ? 64 * nw : 0));  // rank -> lane tables (FP64 form)
@@ -324,8 +324,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   float* ox = (float*)(smem + L.ox);
   float* oy = (float*)(smem + L.oy);
   float* oz = (float*)(smem + L.oz);
-  float* dyt = (float*)(smem + L.dyt);
-  float* dzt = (float*)(smem + L.dzt);
+  float2* dyt = (float2*)(smem + L.dyt);
+  float2* dzt = (float2*)(smem + L.dzt);
   signed char* img = (signed char*)(smem + L.img);
   double* red = (double*)(smem + L.queue);  // scan and reduction scratch, before and after the queues' use
   int* cw = (int*)(smem + L.cw);
@@ -358,9 +358,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   // the far edge of the last ext cell) has origin (g0 + l - 1)*bl + n*r, with
   // n = -1, 0, +1 its periodic image and r = L - nb*bl the extra width of the
   // box's last cell.  o*[l]: origin relative to the tile centre, FP32 (the
-  // multiple of bl is exact, so the value is rounded once).  d*t[l*6 + d + 2]:
-  // origin difference between ext rows l and l + d (d = -2..3), rounded once.
-  // img[32a + l] (FP64 form): n.
+  // multiple of bl is exact, so the value is rounded once).  d*t[l*6 + d + 2]
+  // (y, z): the origin difference between ext rows l and l + d (d = -2..3),
+  // rounded once, and o*[l + d + (d < 0)], the near face of row l + d seen
+  // from row l (the same value as the o* entry).  img[32a + l] (FP64 form): n.
   {
     const int a = tid >> 5, l = tid & 31;
     if (a < 3) {
@@ -379,11 +380,14 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         if (l < E) {
           if (FP64) img[32 * a + l] = (signed char)n;
           if (a > 0) {
-            float* dt = a == 1 ? dyt : dzt;
+            float2* dt = a == 1 ? dyt : dzt;
 #pragma unroll
             for (int d = -2; d <= 3; ++d) {
-              const int l2 = l + d;
-              dt[l * kDT + d + 2] = (l2 >= 0 && l2 <= E) ? fmaf((float)(nimg(l2) - n), rf, (float)d * blf) : 0.f;
+              const int l2 = l + d, ln = l + d + (d < 0);
+              const float off = (l2 >= 0 && l2 <= E) ? fmaf((float)(nimg(l2) - n), rf, (float)d * blf) : 0.f;
+              const float near =
+                  (ln >= 0 && ln <= E) ? fmaf((float)(2 * (ln - 1) - t), 0.5f * blf, (float)nimg(ln) * rf) : 0.f;
+              dt[l * kDT + d + 2] = make_float2(off, near);
             }
           }
         }
@@ -781,15 +785,16 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         int r = 0, mask = 0;
         if (valid) {
           r = sown->rlist[cls][kParts * (k - s_q) + part];
-          mask = sown->lut[cls][r];
+          mask = sown->lut[cls][kParts * (k - s_q) + part];
         }
         int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
         float cy = 0.f, cz = 0.f;
         if (mask) {
           const int dy = srows[2 * r], dz = srows[2 * r + 1];
           const int rowbase = ((ly + dy) + EY * (lz + dz)) * EX + lx - 2;  // + bit b -> ext cell of dx = b - 2
-          cy = dyt[ly * kDT + dy + 2];
-          cz = dzt[lz * kDT + dz + 2];
+          const float2 ry = dyt[ly * kDT + dy + 2], rz = dzt[lz * kDT + dz + 2];
+          cy = ry.x;
+          cz = rz.x;
           if (COUNT) {  // every atom of the owned cells, as the reference visits them
             for (int b = 0; b < 5; ++b)
               if ((mask >> b) & 1) {
@@ -798,9 +803,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
               }
           }
           // distance from the atom to the row's cell boxes
-          // (one table load per axis: the row's near face is ext coordinate
-          // l + d for d > 0 and l + d + 1 for d < 0)
-          const float ty = oy[ly + dy + (dy < 0)] - py, tz = oz[lz + dz + (dz < 0)] - pz;
+          // (the row's near face comes with its origin offset)
+          const float ty = ry.y - py, tz = rz.y - pz;
           const float gy = dy == 0 ? 0.f : fmaxf(dy > 0 ? ty : -ty, 0.f);
           const float gz = dz == 0 ? 0.f : fmaxf(dz > 0 ? tz : -tz, 0.f);
           const float g2 = gy * gy + gz * gz;
@@ -884,7 +888,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         int r = 0, mask = 0;
         if (valid) {
           r = sown->rlist[cls][kCellParts * (k - s_q) + part];
-          mask = sown->lut[cls][r];
+          mask = sown->lut[cls][kCellParts * (k - s_q) + part];
         }
         int lo1 = 0, n1 = 0, lo2 = 0, n2 = 0;
         bool self = false;

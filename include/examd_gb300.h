@@ -218,7 +218,7 @@ int examd_gpu_counters(examd_ctx *ctx, int64_t *candidates, int64_t *accepted,
 /* Introspection (no counterpart in the reference): the row structure and the
  * per-position-class ownership masks the pair kernel derives from the 63-entry
  * table (SRC/exaMD_module.f90:276-346).  rows: 13*2 (dy, dz); lut: 125*13
- * masks over dx = -2..2.  Host-only; returns EXAMD_ERR_ARG if the table does
+ * masks over dx = -2..2, lut[class*13 + row].  Host-only; returns EXAMD_ERR_ARG if the table does
  * not have the expected shape. */
 int examd_own_table(signed char *rows, unsigned char *lut);
 
