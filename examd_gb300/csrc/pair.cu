@@ -584,8 +584,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     __syncwarp();
     // distance tests; accepted pairs go to the queue
     int qb = 0;  // items that start before K
-    for (int K = 0; K < T; K += 32) {
-      const unsigned M = __reduce_or_sync(FULL, (nt > 0 && (unsigned)(s0 - K) < 32u) ? 1u << (s0 - K) : 0u);
+    const int sw = nt > 0 ? s0 >> 5 : -1;  // the 32-candidate window in which the item starts
+    const unsigned sbit = 1u << (s0 & 31);
+    for (int K = 0, kw = 0; K < T; K += 32, ++kw) {
+      const unsigned M = __reduce_or_sync(FULL, sw == kw ? sbit : 0u);
       const int qr = qb + __popc(M & le) - 1;  // >= 0: the first item starts at 0
       qb += __popc(M);
       const float4 a = ptA[qr];
@@ -614,7 +616,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int kb = __float_as_int(a.w);
       if (COUNT && valid) ++neval;
       const float thr = MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
-      const int key = MULTI ? kb | (m << 14) | (tj << 30) : kb | (m << 14);
+      // disjoint bit fields: the sum is the OR, in one instruction
+      const int key = (int)((unsigned)kb + ((unsigned)m << 14) + (MULTI ? (unsigned)tj << 30 : 0u));
       if (MODE == kRedoBig)
         redo_pair(valid && dq.w <= thr, dq, key);
       else
@@ -654,8 +657,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     }
     __syncwarp();
     int qb = 0;  // items that start before K
-    for (int K = 0; K < T; K += 32) {
-      const unsigned M = __reduce_or_sync(FULL, (nt > 0 && (unsigned)(s0 - K) < 32u) ? 1u << (s0 - K) : 0u);
+    const int sw = nt > 0 ? s0 >> 5 : -1;  // the 32-candidate window in which the item starts
+    const unsigned sbit = 1u << (s0 & 31);
+    for (int K = 0, kw = 0; K < T; K += 32, ++kw) {
+      const unsigned M = __reduce_or_sync(FULL, sw == kw ? sbit : 0u);
       const int qr = qb + __popc(M & le) - 1;  // >= 0: the first item starts at 0
       qb += __popc(M);
       const int ql = r2l[32 + qr];
@@ -750,8 +755,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       }
       __syncwarp();
       int qb = 0;  // working atoms that start before K
-      for (int K = 0; K < W; K += 32) {
-        const unsigned M = __reduce_or_sync(FULL, (aw > 0 && (unsigned)(as0 - K) < 32u) ? 1u << (as0 - K) : 0u);
+      const int aww = aw > 0 ? as0 >> 5 : -1;  // the 32-item window in which the atom's items start
+      const unsigned abit = 1u << (as0 & 31);
+      for (int K = 0, kw = 0; K < W; K += 32, ++kw) {
+        const unsigned M = __reduce_or_sync(FULL, aww == kw ? abit : 0u);
         const int qr = qb + __popc(M & (FULL >> (31 - lane))) - 1;  // >= 0: the first worker starts at 0
         qb += __popc(M);
         const int k = K + lane;
@@ -874,8 +881,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int ageo = ex | (ey << 5) | (ez << 10) | (acls << 15);
       const int apa = ai0 | (ana << 16);
       int qb = 0;
-      for (int K = 0; K < W; K += 32) {
-        const unsigned M = __reduce_or_sync(FULL, (aw > 0 && (unsigned)(as0 - K) < 32u) ? 1u << (as0 - K) : 0u);
+      const int aww = aw > 0 ? as0 >> 5 : -1;  // the 32-item window in which the cell's items start
+      const unsigned abit = 1u << (as0 & 31);
+      for (int K = 0, kw = 0; K < W; K += 32, ++kw) {
+        const unsigned M = __reduce_or_sync(FULL, aww == kw ? abit : 0u);
         const int qr = qb + __popc(M & le) - 1;
         qb += __popc(M);
         const int k = K + lane;
