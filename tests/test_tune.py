@@ -1,5 +1,6 @@
 """examd_autotune: the tile shape and CTA width picked by timing, with a text cache."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -39,3 +40,39 @@ def test_tuned_choice_cached_and_equivalent(gpulib, tmp_path, precision, tol):
         g, _, _ = s.forces()
     fr = np.sqrt((g * g).sum(1).mean())
     assert np.sqrt(((f - g) ** 2).sum(1)).max() / fr <= tol
+
+
+def test_cache_hit_needs_no_device(gpulib, tmp_path):
+    """A cached choice is returned without timing (so without a device): tile,
+    warps and tile split come from the cache line; entries written before the
+    tile split existed (five fields, no "|tb" key) are not used."""
+    from examd_gb300 import _lib
+    L = np.array([107.49, 107.49, 107.49])
+    n = 1048576
+    p = _lib.Params()
+    _lib.load().examd_default_params(C.byref(p))
+    p.precision = _lib.MIXED
+    box = (_lib.Box * 1)()
+    for a in range(3):
+        box[0].L[a] = L[a]
+    box[0].natoms = n
+    # the key as examd_autotune forms it; the device name is "unknown" where none can be queried
+    ctx = C.c_void_p()
+    if _lib.load().examd_gpu_create(C.byref(p), 1, box, C.byref(ctx)) != _lib.ERR_NO_DEVICE:
+        _lib.load().examd_gpu_destroy(ctx)
+        pytest.skip("the device name in the key is only predictable without a device")
+    lg = np.round(np.log2(n) * 4.0) / 4.0
+    rho = np.round(n / L.prod() * 20.0) / 20.0
+    key = f"unknown|mixed|nt1|rc2.5|boxes1|n{lg:.2f}|rho{rho:.2f}"
+    cache = tmp_path / "tune.txt"
+    cache.write_text(f"{key}|5 5 5 8 0.5\n"                 # old format: ignored
+                     f"{key}|tb|6 6 6 8 0.41 1\n"
+                     f"{key}|tb|5 4 4 4 0.42 0\n"
+                     f"{key}|tb|6 6 5 8 0.40 1\n")          # the last entry wins
+    best = _lib.Params()
+    ms = C.c_double()
+    pos = np.zeros((n, 3))
+    rc = _lib.load().examd_autotune(C.byref(p), 1, box, n, pos.ctypes.data_as(C.POINTER(C.c_double)), None,
+                                    os.fsencode(str(cache)), C.byref(best), C.byref(ms))
+    assert rc == _lib.OK
+    assert tuple(best.tile) == (6, 6, 5) and best.warps == 8 and best.tile_balance == 1 and ms.value == 0.40
