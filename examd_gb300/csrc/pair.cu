@@ -102,7 +102,7 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.ox = o;     o = align16(o + 4 * (ext_max + 1));
   L.oy = o;     o = align16(o + 4 * (ext_max + 1));
   L.oz = o;     o = align16(o + 4 * (ext_max + 1));
-  L.dyt = o;    o = align16(o + 8 * ext_max * kDT);
+  L.dyt = o;    o = align16(o + 8 * ext_max * kDT);  // float2 (row origin offset, near face) per (l, d)
   L.dzt = o;    o = align16(o + 8 * ext_max * kDT);
   L.img = o;    o = align16(o + (fp64 ? 3 * 32 : 0));  // periodic image per ext coordinate (FP64 form)
   L.cw = o;     o = align16(o + 16);  // unit counter, large-term flag, staged-atom total
