@@ -102,6 +102,8 @@ def load():
             "examd_gpu_strerror": (C.c_char_p, [C.c_int]),
             "examd_gpu_last_error": (C.c_char_p, [ctxp]),
             "examd_own_table": (C.c_int, [C.POINTER(C.c_byte), C.POINTER(C.c_ubyte)]),
+            "examd_tile_split": (C.c_int, [C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int)]),
             "examd_host_alloc": (C.c_int, [C.POINTER(vp), C.c_int64]),
             "examd_host_free": (C.c_int, [vp]),
             "examd_read_particles": (C.c_int, [C.c_char_p, i64p, dp, dp, C.c_int64]),

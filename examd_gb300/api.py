@@ -21,7 +21,7 @@ from . import _lib as _L
 from ._lib import ExamdError, check
 
 __all__ = ["MidpointLJ", "forces_midpoint_all", "gen_fcc", "gen_velocities", "gen_random", "gen_jittered_sc",
-           "pinned_empty", "own_table", "ExamdError", "FP64", "MIXED"]
+           "pinned_empty", "own_table", "tile_split", "ExamdError", "FP64", "MIXED"]
 
 FP64 = "fp64"
 MIXED = "mixed"
@@ -350,6 +350,17 @@ def own_table():
     check(lib.examd_own_table(rows, lut), "examd_own_table")
     return (np.frombuffer(bytes(rows), dtype=np.int8).reshape(13, 2).copy(),
             np.frombuffer(bytes(lut), dtype=np.uint8).reshape(125, 13).copy())
+
+
+def tile_split(nb, last_width, tile_len, tile_balance=0):
+    """Tile starts along one axis of nb cells, as examd_gpu_create splits it
+    (examd_tile_split): nt + 1 ints, the last one nb."""
+    lib = _L.load()
+    starts = (C.c_int * (nb // 2 + 2))()
+    nt = C.c_int()
+    check(lib.examd_tile_split(int(nb), float(last_width), int(tile_len), int(tile_balance), starts, C.byref(nt)),
+          "examd_tile_split")
+    return np.array(starts[:nt.value + 1], dtype=np.int64)
 
 
 def pinned_empty(shape, dtype=np.float64):

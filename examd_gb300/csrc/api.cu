@@ -120,7 +120,31 @@ int round_block_length(double want, double* out, int* q_out, int* k_out) {
   return EXAMD_OK;
 }
 
+// Split of one box axis of nb cells into tiles of at most tile_len cells (an
+// even split: tile_len or tile_len - 1 cells), so that the largest staged
+// tile, which sizes shared memory, stays (tile_len + 2)^3 cells; every tile
+// keeps >= 2 cells.  balance = 1: a last cell at least 1.5 edges wide (it
+// absorbs the remainder of L / edge) counts as two cells in the split, so the
+// tile that holds it has one cell fewer.  Writes nt + 1 starts, returns nt.
+int split_axis(int nb, double last_width, int tile_len, int balance, int* starts) {
+  const int nv = nb + (balance == 1 && last_width >= 1.5 ? 1 : 0);
+  const int nt = std::max(1, std::min(nb / 2, (nv + tile_len - 1) / tile_len));
+  for (int k = 0; k < nt; ++k) starts[k] = (int)((int64_t)k * nv / nt);
+  starts[nt] = nb;
+  if (nt > 1 && starts[nt] - starts[nt - 1] < 2)  // keep >= 2 cells: the even split
+    for (int k = 0; k <= nt; ++k) starts[k] = (int)((int64_t)k * nb / nt);
+  return nt;
+}
+
 }  // namespace
+
+int examd_tile_split(int nb, double last_width, int tile_len, int tile_balance, int* starts, int* nt) {
+  if (!starts || !nt || nb < 1 || nb >= 1024 || tile_len < 1 || tile_balance < 0 || tile_balance > 1 ||
+      !(last_width >= 1.0) || !(last_width < 2.0))
+    return EXAMD_ERR_ARG;
+  *nt = split_axis(nb, last_width, tile_len, tile_balance, starts);
+  return EXAMD_OK;
+}
 
 constexpr int kIoChunks = 4;            // host <-> device transfers of the force call, in chunks
 constexpr int64_t kIoMinChunk = 1 << 16;  // atoms; smaller calls use fewer chunks
@@ -548,18 +572,8 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     }
     int starts[3][1025];
     for (int a = 0; a < 3; ++a) {
-      // tiles of at most Tb cells (Tb or Tb - 1 when nb is not a multiple), so
-      // the largest staged tile, which sizes shared memory, stays (Tb + 2)^3
-      // cells; every tile keeps >= 2 cells.  tile_balance = 1: a last cell at
-      // least 1.5 edges wide counts as two cells (nv = nb + 1 in the split),
-      // so the tile that holds it has one cell fewer
       const double wide = (B.L[a] - (B.nb[a] - 1) * bl) / bl;  // the last cell's width in edges
-      const int nv = B.nb[a] + (p.tile_balance == 1 && wide >= 1.5 ? 1 : 0);
-      B.nt[a] = std::max(1, std::min(B.nb[a] / 2, (nv + Tb[a] - 1) / Tb[a]));
-      for (int k = 0; k < B.nt[a]; ++k) starts[a][k] = (int)((int64_t)k * nv / B.nt[a]);
-      starts[a][B.nt[a]] = B.nb[a];
-      if (B.nt[a] > 1 && starts[a][B.nt[a]] - starts[a][B.nt[a] - 1] < 2)  // keep >= 2 cells: even split
-        for (int k = 0; k <= B.nt[a]; ++k) starts[a][k] = (int)((int64_t)k * B.nb[a] / B.nt[a]);
+      B.nt[a] = split_axis(B.nb[a], wide, Tb[a], p.tile_balance, starts[a]);
       for (int k = 0; k < B.nt[a]; ++k)
         if (starts[a][k + 1] - starts[a][k] + 2 > kMaxExt) {
           delete ctx;

@@ -222,6 +222,14 @@ int examd_gpu_counters(examd_ctx *ctx, int64_t *candidates, int64_t *accepted,
  * not have the expected shape. */
 int examd_own_table(signed char *rows, unsigned char *lut);
 
+/* Introspection: the split of one box axis of nb cells (nb < 1024) into tiles
+ * of at most tile_len cells that examd_gpu_create uses (tile_balance as in
+ * examd_params; last_width: the last cell's width in cell edges, in [1, 2)).
+ * starts: room for nb/2 + 2 ints; receives *nt + 1 tile starts, the last one
+ * nb.  Host-only. */
+int examd_tile_split(int nb, double last_width, int tile_len, int tile_balance,
+                     int *starts, int *nt);
+
 /* Text of a status code; never NULL. */
 const char *examd_gpu_strerror(int code);
 

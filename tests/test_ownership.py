@@ -22,10 +22,9 @@ def pos_class(l, t):
     return 0 if l < 0 else (1 if l == 0 else (2 if l < t - 1 else (3 if l == t - 1 else 4)))
 
 
-def tiles_1d(nb, T):
-    nt = max(1, min(nb // 2, (nb + T - 1) // T))  # the library's partition rule
-    st = [k * nb // nt for k in range(nt + 1)]
-    return [(st[k], st[k + 1] - st[k]) for k in range(nt)]
+def tiles_1d(gpulib, nb, T, width=1.0, balance=0):
+    st = gpulib.tile_split(nb, width, T, balance)  # the library's split of an axis
+    return [(int(st[k]), int(st[k + 1] - st[k])) for k in range(len(st) - 1)]
 
 
 def test_rows_and_table_shape(gpulib, oracle):
@@ -47,9 +46,13 @@ def test_rows_and_table_shape(gpulib, oracle):
     assert lut[2 * 25 + 2 * 5 + 2, 12] == 0b11100
 
 
-@pytest.mark.parametrize("nb,T", [((5, 5, 5), (2, 2, 2)), ((7, 8, 9), (2, 3, 4)), ((9, 6, 11), (3, 2, 5)),
-                                  ((6, 7, 5), (6, 7, 5)), ((10, 10, 10), (4, 4, 4))])
-def test_each_cell_pair_owned_once(gpulib, oracle, nb, T):
+@pytest.mark.parametrize("nb,T,width,balance", [
+    ((5, 5, 5), (2, 2, 2), (1.0,) * 3, 0), ((7, 8, 9), (2, 3, 4), (1.0,) * 3, 0),
+    ((9, 6, 11), (3, 2, 5), (1.0,) * 3, 0), ((6, 7, 5), (6, 7, 5), (1.0,) * 3, 0),
+    ((10, 10, 10), (4, 4, 4), (1.0,) * 3, 0),
+    # split by width: wide last cells on two axes shorten the tiles that hold them
+    ((11, 9, 13), (4, 3, 5), (1.7, 1.2, 1.9), 1), ((7, 8, 9), (3, 3, 3), (1.6, 1.6, 1.6), 1)])
+def test_each_cell_pair_owned_once(gpulib, oracle, nb, T, width, balance):
     rows, lut = gpulib.own_table()
     nb = np.array(nb)
     tab = oracle.midpoint_table()
@@ -59,7 +62,8 @@ def test_each_cell_pair_owned_once(gpulib, oracle, nb, T):
         d = tuple(slot_off(b) - slot_off(a))
         home_of[d] = -slot_off(a)
     cover = {}
-    tiles = [(x, y, z) for z in tiles_1d(nb[2], T[2]) for y in tiles_1d(nb[1], T[1]) for x in tiles_1d(nb[0], T[0])]
+    ax = [tiles_1d(gpulib, nb[a], T[a], width[a], balance) for a in range(3)]
+    tiles = [(x, y, z) for z in ax[2] for y in ax[1] for x in ax[0]]
     lin = lambda c: int(c[0] + nb[0] * (c[1] + nb[1] * c[2]))
     for (x0, tx), (y0, ty), (z0, tz) in tiles:
         org = np.array([x0, y0, z0])
