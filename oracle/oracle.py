@@ -168,8 +168,10 @@ def forces_bruteforce(pos, box, rc, eps=1.0, sigma=1.0, types=None, ntypes=1):
 
 
 def vv_run(pos, vel, box, rc, dt, nsteps, eps=1.0, sigma=1.0, types=None, ntypes=1, mass=None,
-           block_length=None, threads=1):
-    """FP64 velocity-Verlet over the oracle's forces.  Returns dict(pos, vel, forces, ekin[], epot[])."""
+           block_length=None, threads=1, forces=None):
+    """FP64 velocity-Verlet over the oracle's forces.  Returns dict(pos, vel, forces, ekin[], epot[]).
+    forces: the forces at pos (e.g. a previous run's), else computed first; either way the run
+    makes exactly nsteps force evaluations after that."""
     p = _pos(pos).copy()
     v = _pos(vel).copy()
     n = p.shape[0]
@@ -177,7 +179,8 @@ def vv_run(pos, vel, box, rc, dt, nsteps, eps=1.0, sigma=1.0, types=None, ntypes
     bl = 0.5 * float(r.max()) if block_length is None else block_length
     t = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
     m = None if mass is None else np.ascontiguousarray(np.broadcast_to(mass, (ntypes,)), dtype=np.float64)
-    f0 = forces_typed(p, box, rc, eps, sigma, types, ntypes, bl, threads)["forces"].copy()
+    f0 = (forces_typed(p, box, rc, eps, sigma, types, ntypes, bl, threads)["forces"].copy() if forces is None
+          else _pos(forces).copy())
     en = np.zeros(2 * max(nsteps, 1))
     code = lib().exo_vv_run(n, _d(p), _d(v), _i(t) if t is not None else None, _d(m) if m is not None else None,
                             _d(np.asarray(box, dtype=np.float64)), bl, ntypes, _d(e), _d(s), _d(r), dt, nsteps,

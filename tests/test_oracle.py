@@ -180,6 +180,21 @@ def test_vv_energy_conservation(oracle):
     assert np.abs(e - e[0]).max() / abs(e[0]) < 2e-3
 
 
+def test_vv_continues_from_given_forces(oracle):
+    """A run started from a previous run's state and forces continues the same
+    trajectory bit for bit (no extra force evaluation at the start)."""
+    L = np.array([9.0, 9.5, 10.0])
+    rng = np.random.default_rng(5)
+    pos = np.stack(np.meshgrid(*[np.arange(0.3, x, 1.12) for x in L], indexing="ij"), -1).reshape(-1, 3)
+    pos = (pos + rng.uniform(-0.05, 0.05, pos.shape)) % L
+    vel = rng.normal(0, 0.8, pos.shape)
+    whole = oracle.vv_run(pos, vel, L, 2.5, 0.004, 12)
+    a = oracle.vv_run(pos, vel, L, 2.5, 0.004, 5)
+    b = oracle.vv_run(a["pos"], a["vel"], L, 2.5, 0.004, 7, forces=a["forces"])
+    assert np.array_equal(b["pos"], whole["pos"]) and np.array_equal(b["vel"], whole["vel"])
+    assert np.array_equal(np.concatenate([a["epot"], b["epot"]]), whole["epot"])
+
+
 def test_golden_fixture(oracle):
     g = np.load(os.path.join(HERE, "golden", "oracle_midpoint_gas.npz"))
     f, c = oracle.forces_midpoint_all(g["pos"], g["box"], float(g["cutoff"]))
