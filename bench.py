@@ -192,7 +192,7 @@ def fp32_peak():
         r = peaks.measure()
         return float(r["fp32_tflops"]), (f"of measured: FFMA issue rate {r['ffma_per_clk_sm']:.1f}/clk/SM at "
                                           f"{r['clock_mhz']:.0f} MHz, python -m examd_gb300.peaks, this run "
-                                          "(the driver-measured peaks have no FP32 figure)")
+                                          "(MEASURED_PEAKS.json holds no FP32 figure)")
     except Exception as e:  # the probe is a measurement aid; the committed figure stands in
         return FP32_PEAK_TFLOPS, f"of measured earlier (profiles/gb300_pipe_rates.txt); live probe failed: {e}"
 
