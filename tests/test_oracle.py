@@ -195,6 +195,20 @@ def test_vv_continues_from_given_forces(oracle):
     assert np.array_equal(np.concatenate([a["epot"], b["epot"]]), whole["epot"])
 
 
+def test_golden_fixture_typed_mixture(oracle):
+    """The typed oracle reproduces its committed two-type fixture bit for bit,
+    and an independent O(N^2) minimum-image sum agrees with it."""
+    g = np.load(os.path.join(HERE, "golden", "oracle_typed_mixture.npz"))
+    t = oracle.forces_typed(g["pos"], g["box"], g["rc"], g["eps"], g["sigma"], g["types"], 2)
+    np.testing.assert_array_equal(t["forces"], g["forces"])
+    assert t["epot"] == float(g["epot"]) and t["virial"] == float(g["virial"])
+    assert t["counts"].candidates == int(g["candidates"]) and t["counts"].accepted == int(g["accepted"])
+    b = oracle.forces_bruteforce(g["pos"], g["box"], g["rc"], g["eps"], g["sigma"], g["types"], 2)
+    s = np.sqrt((g["forces"] ** 2).sum(1).mean())
+    assert np.sqrt(((b["forces"] - g["forces"]) ** 2).sum(1)).max() / s <= 1e-12
+    assert abs(b["epot"] - float(g["epot"])) <= 1e-12 * abs(float(g["epot"]))
+
+
 def test_golden_fixture(oracle):
     g = np.load(os.path.join(HERE, "golden", "oracle_midpoint_gas.npz"))
     f, c = oracle.forces_midpoint_all(g["pos"], g["box"], float(g["cutoff"]))
