@@ -34,3 +34,25 @@ def test_reference_arm_other_workloads_say_unavailable():
     assert r.returncode == 0
     d = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
     assert d["impl"] == "reference" and "unavailable" in d
+
+
+def test_gpu_arm_fails_loudly_without_a_device():
+    """Without an sm_103 GPU the benchmark's own arm stops with the library's
+    no-device status and prints no result line: there is no CPU fallback."""
+    import ctypes as C
+    from examd_gb300 import _lib
+    p = _lib.Params()
+    _lib.load().examd_default_params(C.byref(p))
+    box = (_lib.Box * 1)()
+    for a in range(3):
+        box[0].L[a] = 20.0
+    box[0].natoms = 10
+    ctx = C.c_void_p()
+    if _lib.load().examd_gpu_create(C.byref(p), 1, box, C.byref(ctx)) != _lib.ERR_NO_DEVICE:
+        _lib.load().examd_gpu_destroy(ctx)
+        return  # a device is present: nothing to check here
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--steps", "1", "--warmup", "3"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode != 0
+    assert "no usable sm_103 CUDA device" in r.stderr
+    assert not [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
