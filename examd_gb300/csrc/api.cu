@@ -1220,9 +1220,16 @@ int ensure_ebuf(examd_ctx* ctx, int steps) {
   if ((rc = dalloc(ctx, &ctx->boxE, n)) || (rc = dalloc(ctx, &ctx->boxW, n)) || (rc = dalloc(ctx, &ctx->boxKE, n)))
     return rc;
   ctx->ebuf_steps = steps;
+  // every captured graph that names the old energy buffers is stale: the step
+  // loop's and the force call's (whose energy variant writes and reads boxE,
+  // boxW)
   if (ctx->gexec) {
     cudaGraphExecDestroy(ctx->gexec);
     ctx->gexec = nullptr;
+  }
+  for (auto& g : ctx->io_graph) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = examd_ctx::IoGraph{};
   }
   return EXAMD_OK;
 }

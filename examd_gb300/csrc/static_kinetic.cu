@@ -26,7 +26,10 @@
 //     stream before it returns;
 //   * the first call on a device resolves the array's address with
 //     cudaGetSymbolAddress (this loads the module).  Make that first call
-//     before any stream capture begins.
+//     before any stream capture begins.  The address is cached for the life
+//     of the process: a cudaDeviceReset of that device unloads the module and
+//     leaves the cached address stale, so this entry point must not be used
+//     on a device after the caller resets it.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -218,6 +221,14 @@ extern "C" int examd_kinetic_static(int device, int64_t natoms, int nboxes, cons
       put_err(errbuf, errbuf_len, "a type index is outside [0, ntypes)");
       rc = EXAMD_ERR_ARG;
     }
+  }
+  // On a failure after work was queued, wait for that work before returning,
+  // so that no kernel or copy of this call still touches the shared array when
+  // the next call (perhaps on another stream) starts.  The wait's own result
+  // is ignored: the status already reports the first failure.
+  if (rc != EXAMD_OK) {
+    cudaStreamSynchronize(st);
+    cudaGetLastError();
   }
   cudaSetDevice(prev >= 0 ? prev : device);
   return rc;

@@ -38,7 +38,8 @@ extern "C" {
 #define EXAMD_ERR_NB_TOO_SMALL 202  /* fewer than 5 cells on an axis          */
 #define EXAMD_ERR_CELL_OVERFLOW 203 /* a tile's staged atoms exceed capacity  */
 #define EXAMD_ERR_NONFINITE 204     /* NaN/Inf position or force              */
-#define EXAMD_ERR_TIMEOUT 205       /* a bounded device wait gave up          */
+#define EXAMD_ERR_TIMEOUT 205       /* a bounded device wait gave up (reserved:
+                                       no current kernel waits on another CTA) */
 #define EXAMD_ERR_CUDA 206          /* CUDA runtime error                     */
 #define EXAMD_ERR_NOMEM 207         /* device or pinned allocation failed     */
 #define EXAMD_ERR_STATE 208         /* call order (e.g. no atoms set)         */
@@ -167,7 +168,11 @@ int examd_gpu_kinetic(examd_ctx *ctx, double *ekin);
  *   - every call shares that array: calls whose device work overlaps (other
  *     threads, or unordered streams) race; sequential calls are safe;
  *   - the first call on a device sets up the array's address
- *     (cudaGetSymbolAddress); make it before any stream capture begins.
+ *     (cudaGetSymbolAddress); make it before any stream capture begins.  The
+ *     address is kept for the life of the process: do not call this entry
+ *     point on a device after a cudaDeviceReset of it;
+ *   - a call that fails after queueing device work waits for that work before
+ *     it returns, so sequential calls stay safe on error paths too.
  * atom0: host, nboxes+1 offsets (0 .. natoms) of each box's contiguous atoms.
  * vx, vy, vz: device, natoms doubles each.  type: device, natoms ints in
  * [0, ntypes), or NULL for all type 0.  mass: host, ntypes doubles.  ekin:

@@ -48,3 +48,31 @@ def test_graph_replay_equals_eager(gpulib, case):
         assert np.array_equal(ea, eb) and np.array_equal(wa, wb)
     assert np.array_equal(again, eager[0][0])
     assert np.array_equal(acc, eager[0][0] + 1.0)
+
+
+def test_graph_replay_with_energy_across_a_run(gpulib, case):
+    """The energy variant of the captured force call, with the same pinned
+    buffers before and after a run: the run reallocates the per-box energy
+    buffers (its first call sizes them for its graph chunk), so the force
+    call must capture again instead of replaying a graph that names the old
+    ones."""
+    kw = dict(precision="mixed", **case["lj"])
+    p0 = case["pos"]
+    with gpulib.MidpointLJ(case["boxes"], case["natoms"], **kw) as s:
+        s.set_atoms(p0)
+        f_ref, e_ref, w_ref = s.forces_at(p0, energy=True)
+    hp = gpulib.pinned_empty(p0.shape)
+    hf = gpulib.pinned_empty(p0.shape)
+    with gpulib.MidpointLJ(case["boxes"], case["natoms"], **kw) as s:
+        s.set_atoms(p0)
+        hp[:] = p0
+        for _ in range(3):  # capture at both parities, then a replay
+            _, e, w = s.forces_at(hp, out=hf, energy=True)
+        assert np.array_equal(hf, f_ref) and np.array_equal(e, e_ref) and np.array_equal(w, w_ref)
+        s.run(4, 0.001, graph_chunk=2)
+        for _ in range(3):
+            _, e, w = s.forces_at(hp, out=hf, energy=True)
+            assert np.array_equal(hf, f_ref) and np.array_equal(e, e_ref) and np.array_equal(w, w_ref)
+        s.run(6, 0.001, graph_chunk=4)  # grows the energy buffers again
+        _, e, w = s.forces_at(hp, out=hf, energy=True)
+        assert np.array_equal(hf, f_ref) and np.array_equal(e, e_ref) and np.array_equal(w, w_ref)
