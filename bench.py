@@ -1,32 +1,43 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 midpoint Lennard-Jones path (one JSON line on stdout).
 
-Default workload: 1,048,576 atoms (FCC 64^3 x 4) at rho* = 0.8442, melted at
-T* = 1.0, LJ eps = sigma = m = 1, rc = 2.5 sigma truncated and unshifted,
-dt = 0.005, velocity-Verlet with re-binning every step.  A step = one
-velocity-Verlet step over all atoms (kick + drift + wrap + binning + midpoint
-pair forces).  Synthetic, seeded inputs; no dataset is involved.
+Default workload: the largest configuration that fits one GPU, 16,777,216
+atoms of an 80:20 two-species LJ mixture (Kob-Andersen-type table eps_AA = 1,
+sigma_AA = 1, eps_AB = 1.5, sigma_AB = 0.8, eps_BB = 0.5, sigma_BB = 0.88,
+cutoff 2.5 sigma_ab per pair) on a jittered simple-cubic lattice at rho* =
+1.2, T* = 1.0, dt = 0.003.  A step = one velocity-Verlet step over all atoms
+(kick + drift + wrap + binning + midpoint pair forces).  Synthetic, seeded
+inputs built by examd_gb300/workloads.py (plain numpy); no dataset is
+involved.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl examd|reference]
-                    [--workload liquid|liquid-rc3|slab|ensemble|mixture|fcc32k]
+                    [--workload mixture|liquid|liquid-rc3|slab|ensemble|fcc32k]
+
+Both arms time the same state: the workload's seeded atoms after W warm-up
+steps, then K timed steps.
 
 value: atom-steps/s of the mixed form with all state resident in HBM, device
-time (CUDA events on the library's stream), max over ranks.  e2e: the same
+time (CUDA events on the library's stream, the step loop replayed as CUDA
+graphs captured before the timed region), max over ranks.  e2e: the same
 metric through the drop-in force call with host buffers (pinned positions in,
-forces out, every step).  The line also carries the FP64 form's rate on the
-same atoms, the mixed form's force error against it and both forms' energy
-drift per 1000 steps.  --impl reference times the CPU restatement of the
-reference's force routine (oracle/) with all host threads on the same
-workload.  With N > 1 (torchrun) each rank runs an independent replica on its
-own GPU (the path has no inter-GPU exchange): scaling "weak".
+forces out, every step).  The line also carries the pair kernel's roofline,
+per-phase times, the CPU baseline (the oracle on the machine's host cores), and,
+on a separately equilibrated state, the FP64 form's rate at its own tuned
+tiles, the mixed form's force error against it and both forms' energy drift.
+--impl reference times the CPU restatement of the reference's force routine
+(oracle/) with all host threads on the same workload and state, loading no
+library of the product.  With N > 1 (torchrun) each rank runs an independent
+replica on its own GPU (the path has no inter-GPU exchange): scaling "weak".
 
 Other workloads (--workload) are the remaining configurations of the same
-metric: rc = 3.0; an uneven liquid slab in vapour; a batched ensemble of 512
-boxes; a 16.8M-atom binary mixture; the 32,000-atom FCC fluid at T* = 0.72.
+metric: the 1,048,576-atom liquid at rc 2.5 and 3.0; an uneven liquid slab in
+vapour; a batched ensemble of 512 boxes; the 32,000-atom FCC crystal at T* =
+0.72.
 """
 from __future__ import annotations
 
 import argparse
+import importlib.util
 import json
 import os
 import re
@@ -39,19 +50,54 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-NC, RHO, RC, DT, T_MELT = 64, 0.8442, 2.5, 0.005, 1.0
 METRIC = "atom-steps/s on 1 GB300: mixed-FP32 vs FP64 path at <=1e-5 RMS force rel. error"
 FP32_PEAK_TFLOPS = 73.84  # FFMA probe (python -m examd_gb300.peaks) on a GB300; used if the live probe fails
 
-# name -> (workload label, dt, equilibration steps, rescale interval, drift steps)
+# name -> workload label, generator name and arguments, dt, equilibration steps (velocity rescaling every
+# `every` steps), steps of NVE before the drift window, drift window
 WORKLOADS = {
-    "liquid": ("lj-liquid-fcc64-1048576-rc2.5", 0.005, 300, 50, 1000),
-    "liquid-rc3": ("lj-liquid-fcc64-1048576-rc3.0", 0.005, 300, 50, 1000),
-    "slab": ("lj-slab-524288-rho0.75-in-vapour0.02-Lz4Lx-rc3.0", 0.005, 200, 20, 500),
-    "ensemble": ("lj-ensemble-512-boxes-256-16384-rc2.5", 0.005, 200, 20, 1000),
-    "mixture": ("lj-binary-mixture-16777216-80-20-rho1.2-rc2.5sigma", 0.003, 200, 20, 1000),
-    "fcc32k": ("lj-fcc-32000-rho0.8442-T0.72-rc2.5", 0.005, 0, 0, 1000),
+    "mixture": dict(label="lj-binary-mixture-16777216-80-20-rho1.2-rc2.5sigma", gen="binary_mixture",
+                    args={"m": 256, "seed": 5}, dt=0.003, eq=2000, every=20, settle=200, drift=1000),
+    "liquid": dict(label="lj-liquid-fcc64-1048576-rc2.5", gen="liquid_fcc", args={"nc": 64, "rc": 2.5, "seed": 1},
+                   dt=0.005, eq=2000, every=20, settle=200, drift=1000),
+    "liquid-rc3": dict(label="lj-liquid-fcc64-1048576-rc3.0", gen="liquid_fcc",
+                       args={"nc": 64, "rc": 3.0, "seed": 1}, dt=0.005, eq=2000, every=20, settle=200, drift=1000),
+    "slab": dict(label="lj-slab-524288-rho0.75-in-vapour0.02-Lz4Lx-rc3.0", gen="slab", args={"seed": 3},
+                 dt=0.005, eq=2000, every=20, settle=200, drift=500),
+    "ensemble": dict(label="lj-ensemble-512-boxes-256-16384-rc2.5", gen="ensemble", args={"seed": 4},
+                     dt=0.005, eq=2000, every=20, settle=200, drift=1000),
+    "fcc32k": dict(label="lj-fcc-32000-rho0.8442-T0.72-rc2.5", gen="fcc_lattice", args={"nc": 20, "seed": 1},
+                   dt=0.005, eq=0, every=0, settle=0, drift=1000),
 }
+DEFAULT_WORKLOAD = "mixture"
+
+
+def load_workloads():
+    """examd_gb300/workloads.py by its path: the generators are plain numpy,
+    and loading the file alone keeps the package (and its CUDA library) out
+    of the reference arm's process."""
+    spec = importlib.util.spec_from_file_location("examd_workloads", os.path.join(ROOT, "examd_gb300", "workloads.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def make_case(name):
+    w = WORKLOADS[name]
+    return getattr(load_workloads(), w["gen"])(**w["args"])
+
+
+def config_of(name, case):
+    """The `config` object both arms print (no implementation-specific keys)."""
+    w = WORKLOADS[name]
+    n = int(case["natoms"].sum())
+    lj = case["lj"]
+    rc = lj.get("rc")
+    return {"workload": w["label"], "atoms": n, "boxes": int(len(case["natoms"])),
+            "rc": rc if np.ndim(rc) == 0 else np.asarray(rc).tolist(), "dt": w["dt"],
+            "state": f"{w['gen']}({', '.join(f'{k}={v}' for k, v in w['args'].items())}) then the warm-up steps",
+            "l2": ("working set > L2 (per-step HBM traffic ~0.2 KB per atom)" if n * 200 > 129e6
+                   else "working set fits L2 (small configuration)")}
 
 
 def dist_info():
@@ -81,46 +127,6 @@ def allmax(dist, x):
     t = torch.tensor([x], dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
-
-
-def build_liquid(ex, seed=1):
-    pos, L = ex.gen_fcc(NC, RHO)
-    vel = ex.gen_velocities(len(pos), 2.0 * T_MELT, seed)
-    return pos, vel, L
-
-
-def make_case(name, seed):
-    """Atoms, boxes and LJ parameters of a workload, plus each box's target temperature."""
-    import examd_gb300 as ex
-    from examd_gb300 import workloads as W
-    if name in ("liquid", "liquid-rc3"):
-        pos, vel, L = build_liquid(ex, seed)  # hot start at 2 T*, melted by the equilibration
-        case = {"pos": pos, "vel": vel, "types": None, "boxes": np.full((1, 3), L), "natoms": np.array([len(pos)]),
-                "lj": {"rc": 3.0 if name == "liquid-rc3" else RC}}
-        return case, np.array([T_MELT])
-    if name == "slab":
-        return W.slab(seed=seed + 2), np.array([0.85])
-    if name == "ensemble":
-        c = W.ensemble(seed=seed + 3)
-        return c, c["temperatures"]
-    if name == "mixture":
-        return W.binary_mixture(seed=seed + 4), np.array([1.0])
-    if name == "fcc32k":
-        pos, L = ex.gen_fcc(20, RHO)
-        vel = ex.gen_velocities(len(pos), 0.72, seed)
-        case = {"pos": pos, "vel": vel, "types": None, "boxes": np.full((1, 3), L), "natoms": np.array([len(pos)]),
-                "lj": {"rc": RC}}
-        return case, np.array([0.72])
-    raise ValueError(name)
-
-
-def equilibrate(sysm, natoms, temps, steps, every, dt):
-    """steps velocity-Verlet steps, rescaling each box to its target temperature every `every` steps."""
-    dof = 3.0 * np.maximum(np.asarray(natoms, dtype=np.float64) - 1.0, 1.0)
-    for _ in range(steps // every if every else 0):
-        sysm.run(every, dt)
-        T = 2.0 * sysm.kinetic() / dof
-        sysm.scale_velocities(np.sqrt(temps / np.maximum(T, 1e-12)))
 
 
 class ClockSampler:
@@ -176,13 +182,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def read_traffic():
-    """dram bytes per pair-kernel launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "pair_mixed_fcc64_1048576.md")
+def read_traffic(workload):
+    """DRAM bytes per pair-kernel launch from the committed ncu summary of this workload, if any."""
+    names = {"mixture": "pair_mixed_mixture_16777216.md", "liquid": "pair_mixed_fcc64_1048576.md"}
+    if workload not in names:
+        return None, None
+    p = os.path.join(ROOT, "profiles", names[workload])
     if not os.path.exists(p):
-        return None
+        return None, None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
-    return float(m.group(1)) if m else None
+    return (float(m.group(1)), f"profiles/{names[workload]}") if m else (None, None)
 
 
 def fp32_peak():
@@ -205,61 +214,167 @@ def drift_per_1000(e, scale=None):
     return float(np.polyfit(s, y, 1)[0] * 1000.0)
 
 
-def cpu_baseline(pos, L, reps=2):
+def _oracle_boxes(case):
+    """(pos, types, box) per box of a case, for the oracle (one box at a time)."""
+    a0 = np.concatenate([[0], np.cumsum(case["natoms"])])
+    t = case["types"]
+    for b in range(len(case["natoms"])):
+        yield (case["pos"][a0[b]:a0[b + 1]], None if t is None else t[a0[b]:a0[b + 1]], case["boxes"][b],
+               case["vel"][a0[b]:a0[b + 1]])
+
+
+def _oracle_lj(case):
+    lj = case["lj"]
+    return dict(rc=lj["rc"], eps=lj.get("eps", 1.0), sigma=lj.get("sigma", 1.0), ntypes=lj.get("ntypes", 1))
+
+
+def cpu_baseline(case, budget_s=30.0):
+    """Force evaluations of the oracle (the C restatement of
+    exaMD_forces_midpoint_all) on the given atoms, all host threads: the
+    reference's timed call (exaMD.f90:241-253) turned into atom-steps/s."""
     from oracle import oracle as O
     O.build()
     cores = os.cpu_count() or 1
-    O.forces_typed(pos[: min(len(pos), 20000)], np.full(3, L), RC, threads=cores)  # warm
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        O.forces_typed(pos, np.full(3, L), RC, threads=cores)
-    t = (time.perf_counter() - t0) / reps
-    t1 = time.perf_counter()
-    O.forces_typed(pos, np.full(3, L), RC, threads=1)  # one core, as one reference MPI rank runs
-    t1 = time.perf_counter() - t1
-    return {"value": len(pos) / t, "unit": "atom-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{reps} force evaluations of the {len(pos)}-atom workload by the C restatement of "
-                      f"exaMD_forces_midpoint_all (OpenMP over home blocks, {cores} threads); "
-                      f"{t:.3f} s each; integration O(N) neglected",
-            "single_core": {"value": len(pos) / t1, "cores": 1,
-                            "sample": f"1 force evaluation on one thread, {t1:.3f} s"}}
+    lj = _oracle_lj(case)
+    n = int(case["natoms"].sum())
+
+    def one(threads):
+        t0 = time.perf_counter()
+        for p, t, L, _ in _oracle_boxes(case):
+            O.forces_typed(p, L, types=t, threads=threads, **lj)
+        return time.perf_counter() - t0
+
+    t_first = one(cores)
+    reps = int(max(1, min(3, budget_s // max(t_first, 1e-3))))
+    ts = [one(cores) for _ in range(reps)]
+    t = float(np.mean(ts))
+    out = {"value": n / t, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+           "sample": f"{reps} force evaluations (after one untimed) of the {n}-atom workload on its generated "
+                     f"state by the C restatement of exaMD_forces_midpoint_all (OpenMP over home blocks, "
+                     f"{cores} threads), {t:.3f} s each; integration O(N) neglected"}
+    if t * cores < budget_s:
+        t1 = one(1)
+        out["single_core"] = {"value": n / t1, "cores": 1, "sample": f"1 force evaluation on one thread, {t1:.3f} s"}
+    return out
 
 
 def run_reference(args, ws, rk):
-    """CPU restatement of the reference path, all host threads, same workload."""
+    """The CPU restatement of the reference path, all host threads, on the
+    workload's generated state: W warm-up steps, then timed steps of
+    velocity-Verlet whose forces come from the restated
+    exaMD_forces_midpoint_all.  Loads no library of the product."""
     if rk != 0:
         return
-    if args.workload != "liquid":
-        print(json.dumps({"impl": "reference", "unavailable": f"the CPU arm covers the default workload only, "
-                                                              f"not {args.workload}"}), flush=True)
-        return
-    import examd_gb300 as ex
     from oracle import oracle as O
     O.build()
-    pos, vel, L = build_liquid(ex)
-    rng = np.random.default_rng(7)
-    pos = (pos + rng.uniform(-0.15, 0.15, pos.shape)) % L  # liquid-like disorder without a GPU melt
+    case = make_case(args.workload)
+    w = WORKLOADS[args.workload]
+    dt = w["dt"]
     cores = os.cpu_count() or 1
-    box = np.full(3, L)
-    w = O.vv_run(pos, vel, box, RC, DT, max(args.warmup, 1), threads=cores)
-    # the timed steps continue the warm-up trajectory from its forces: exactly `steps` force evaluations
+    lj = _oracle_lj(case)
+    mass = case["lj"].get("mass")
+    boxes = list(_oracle_boxes(case))
+    n = int(case["natoms"].sum())
+    states = []
     t0 = time.perf_counter()
-    out = O.vv_run(w["pos"], w["vel"], box, RC, DT, args.steps, threads=cores, forces=w["forces"])
+    for p, t, L, v in boxes:
+        r = O.vv_run(p, v, L, dt=dt, nsteps=args.warmup, types=t, mass=mass, threads=cores, **lj)
+        states.append((r["pos"], r["vel"], r["forces"], t, L))
+    t_warm = (time.perf_counter() - t0) / max(args.warmup, 1)
+    # the timed steps continue the warm-up trajectory from its forces: exactly K force evaluations; a step
+    # that would take the run past about 150 s is not started (a bounded sample of the K steps)
+    k_run = int(max(1, min(args.steps, 150.0 // max(t_warm, 1e-6))))
+    t0 = time.perf_counter()
+    for p, v, f, t, L in states:
+        O.vv_run(p, v, L, dt=dt, nsteps=k_run, types=t, mass=mass, threads=cores, forces=f, **lj)
     t = time.perf_counter() - t0
-    v = len(pos) * args.steps / t
-    line = {"metric": METRIC, "value": v, "unit": "atom-steps/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOADS["liquid"][0], "atoms": len(pos), "rc": RC, "dt": DT,
-                       "precision": "fp64", "l2": "working set > L2"},
+    val = n * k_run / t
+    sample = (f"{k_run} velocity-Verlet steps (forces by the C restatement of exaMD_forces_midpoint_all, OpenMP "
+              f"{cores} threads) of the {n}-atom workload after {args.warmup} warm-up steps"
+              + (f"; {k_run} of the {args.steps} requested steps timed, to bound the run" if k_run < args.steps
+                 else ""))
+    line = {"metric": METRIC, "value": val, "unit": "atom-steps/s", "n_gpus": args.gpus, "steps": k_run,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / k_run, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_of(args.workload, case),
             "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} velocity-Verlet steps (force evaluation by the C restatement "
-                                       f"of exaMD_forces_midpoint_all, OpenMP {cores} threads) of the "
-                                       f"{len(pos)}-atom workload"},
-            "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "final_epot": float(out["epot"][-1])}
+            "cpu_baseline": {"value": val, "unit": "atom-steps/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def equilibrate(sysm, natoms, temps, steps, every, dt):
+    """steps velocity-Verlet steps, rescaling each box to its target temperature every `every` steps."""
+    dof = 3.0 * np.maximum(np.asarray(natoms, dtype=np.float64) - 1.0, 1.0)
+    for _ in range(steps // every if every else 0):
+        sysm.run(every, dt, graph_chunk=every)
+        T = 2.0 * sysm.kinetic() / dof
+        sysm.scale_velocities(np.sqrt(temps / np.maximum(T, 1e-12)))
+
+
+def accuracy_and_drift(ex, case, w, lj, tuning, lr, dt):
+    """On an equilibrated state (rescaled, then NVE): the mixed form's force
+    error against the FP64 form, the FP64 form's rate at its own tuned tiles
+    (graph-captured as the mixed form), and both forms' energy drift."""
+    natoms, boxes, types = case["natoms"], case["boxes"], case["types"]
+    nboxes = len(natoms)
+    n = int(natoms.sum())
+    with ex.MidpointLJ(boxes, natoms, precision="mixed", device=lr, **tuning, **lj) as s:
+        s.set_atoms(case["pos"], types, case["vel"])
+        equilibrate(s, natoms, case["temperatures"], w["eq"], w["every"], dt)
+        if w["settle"]:
+            s.run(w["settle"], dt, graph_chunk=20)
+        pos_eq, vel_eq = s.state()
+        f32, e32, _ = s.forces(energy=True)
+        dm = s.run(w["drift"], dt, graph_chunk=50, energies=True)
+        s.set_atoms(pos_eq, types, vel_eq)
+        s.run(4, dt)
+        s.prepare_run(dt, 10)
+        o32 = s.run(20, dt, graph_chunk=10)
+    t64 = ex.autotune(boxes, natoms, pos_eq, types, precision="fp64", device=lr, **lj)
+    tune64 = {"tile": t64["tile"], "warps": t64["warps"], "tile_balance": t64["tile_balance"]}
+    with ex.MidpointLJ(boxes, natoms, precision="fp64", device=lr, **tune64, **lj) as s64:
+        s64.set_atoms(pos_eq, types, vel_eq)
+        f64, e64, _ = s64.forces(energy=True)
+        d64 = s64.run(w["drift"], dt, graph_chunk=50, energies=True)
+        s64.set_atoms(pos_eq, types, vel_eq)
+        s64.run(4, dt)
+        k64 = 20
+        s64.prepare_run(dt, 10)
+        o64 = s64.run(k64, dt, graph_chunk=10)
+    err = np.sqrt(((f32 - f64) ** 2).sum(1))
+    fr = np.sqrt((f64 * f64).sum(1).mean())
+    v64 = n * k64 / (o64["ms"] * 1e-3)
+    v32 = n * 20 / (o32["ms"] * 1e-3)
+    em = dm["ekin"] + dm["epot"]
+    e6 = d64["ekin"] + d64["epot"]
+    drift_m = [drift_per_1000(em[:, b]) for b in range(nboxes)]
+    drift_d = [drift_per_1000(e6[:, b]) for b in range(nboxes)]
+    out = {"fp64": {"value": v64, "ms_per_step": o64["ms"] / k64, "tile": list(tune64["tile"]),
+                    "warps": tune64["warps"], "tile_balance": tune64["tile_balance"], "graph_chunk": 10,
+                    "state": "equilibrated"},
+           "mixed_equilibrated": {"value": v32, "ms_per_step": o32["ms"] / 20, "graph_chunk": 10},
+           "mixed_over_fp64": v32 / v64,
+           "force_rel_err_vs_fp64": {"rms": float(np.sqrt((err * err).mean()) / fr), "max": float(err.max() / fr),
+                                     "state": "equilibrated"},
+           "epot_rel_err_vs_fp64": float(np.abs(e32.sum() - e64.sum()) / abs(e64.sum())),
+           "equilibration": {"steps": w["eq"], "rescale_every": w["every"], "nve_steps": w["settle"]}}
+    if nboxes == 1:
+        out["energy_drift_per_1000_steps"] = {"mixed": drift_m[0], "fp64": drift_d[0], "steps": w["drift"]}
+    else:
+        # a box's total energy can be near zero (gas-like boxes), which makes
+        # (E - E0)/|E0| meaningless there: also report (E - E0)/<Ekin>
+        km, k6 = dm["ekin"].mean(0), d64["ekin"].mean(0)
+        am, ad = np.abs(drift_m), np.abs(drift_d)
+        bm = np.abs([drift_per_1000(em[:, b], km[b]) for b in range(nboxes)])
+        bd = np.abs([drift_per_1000(e6[:, b], k6[b]) for b in range(nboxes)])
+        out["energy_drift_per_1000_steps"] = {
+            "mixed": {"median_abs": float(np.median(am)), "max_abs": float(am.max()),
+                      "median_abs_vs_ekin": float(np.median(bm)), "max_abs_vs_ekin": float(bm.max())},
+            "fp64": {"median_abs": float(np.median(ad)), "max_abs": float(ad.max()),
+                     "median_abs_vs_ekin": float(np.median(bd)), "max_abs_vs_ekin": float(bd.max())},
+            "per_box": "per-box drift; median and max of |drift| over the boxes, relative to |E0| and "
+                       "to the box's mean kinetic energy", "steps": w["drift"]}
+    return out
 
 
 def main():
@@ -268,9 +383,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="examd", choices=["examd", "reference"])
-    ap.add_argument("--workload", default="liquid", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--chunk", type=int, default=20, help="steps per captured CUDA graph")
-    ap.add_argument("--drift-steps", type=int, default=None, help="steps of the energy-drift runs")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 / drift side measurements")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-tune", action="store_true", help="default tile shape instead of the autotuner's")
@@ -286,30 +400,25 @@ def main():
     import examd_gb300 as ex
     from examd_gb300 import build as B
     B.build()
-    label, dt, eq_steps, eq_every, drift_steps = WORKLOADS[args.workload]
-    if args.drift_steps is not None:
-        drift_steps = args.drift_steps
-    case, temps = make_case(args.workload, 1 + rk)
+    w = WORKLOADS[args.workload]
+    dt = w["dt"]
+    case = make_case(args.workload)  # every replica times the same seeded state
     n = int(case["natoms"].sum())
     nboxes = len(case["natoms"])
     lj = dict(case["lj"])
-    sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **lj)
-    sysm.set_atoms(case["pos"], case["types"], case["vel"])
-    equilibrate(sysm, case["natoms"], temps, eq_steps, eq_every, dt)
-    tuning = {"tile": "default", "warps": "default", "tile_balance": 0}
+    tuning = {}
+    tune_info = {"tile": "default", "warps": "default", "tile_balance": 0}
     if not args.no_tune:
-        # tile shape, warps per CTA and tile split for the equilibrated atoms (examd_autotune)
-        pos_eq, vel_eq = sysm.state()
-        tuning = ex.autotune(case["boxes"], case["natoms"], pos_eq, case["types"], precision="mixed", device=lr,
-                             **lj)
-        sysm.close()
-        sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, tile=tuning["tile"],
-                             warps=tuning["warps"], tile_balance=tuning["tile_balance"], **lj)
-        sysm.set_atoms(pos_eq, case["types"], vel_eq)
+        # tile shape, warps per CTA and tile split for these atoms (examd_autotune)
+        t = ex.autotune(case["boxes"], case["natoms"], case["pos"], case["types"], precision="mixed", device=lr,
+                        **lj)
+        tuning = {"tile": t["tile"], "warps": t["warps"], "tile_balance": t["tile_balance"]}
+        tune_info = {"tile": list(t["tile"]), "warps": t["warps"], "tile_balance": t["tile_balance"]}
+    sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **tuning, **lj)
+    sysm.set_atoms(case["pos"], case["types"], case["vel"])
+    sysm.run(args.warmup, dt)  # exactly W untimed steps
     chunk = max(2, args.chunk // 2 * 2)
-    wsteps = max(args.warmup, chunk + 2)
-    wsteps += wsteps % 2
-    sysm.run(wsteps, dt, graph_chunk=chunk)  # warm-up; captures the graph (even count keeps buffer parity)
+    sysm.prepare_run(dt, chunk)  # capture the step-loop graph outside the timed region
 
     barrier(dist)
     with ClockSampler(lr) as clk:
@@ -322,10 +431,9 @@ def main():
     cnt = sysm.counters()
     flops = 8.0 * cnt["candidates"] + 22.0 * cnt["accepted"]
     peak, peak_src = fp32_peak()
-    reps = 20
-    _, k_ms = sysm.time_forces(reps)
+    _, k_ms = sysm.time_forces(20)
     achieved = flops / (k_ms * 1e-3) / 1e12
-    traffic = read_traffic() if args.workload == "liquid" else None
+    traffic, traffic_src = read_traffic(args.workload)
 
     # end to end through the drop-in force call with pinned host buffers
     state, _ = sysm.state()
@@ -333,6 +441,7 @@ def main():
     hp[:] = state
     hf = ex.pinned_empty((n, 3))
     sysm.forces_at(hp, out=hf)
+    sysm.forces_at(hp, out=hf)  # both parities captured
     e2e_steps = max(args.steps // 2, 10)
     barrier(dist)
     t0 = time.perf_counter()
@@ -340,76 +449,34 @@ def main():
         sysm.forces_at(hp, out=hf)
     t_e2e = allmax(dist, time.perf_counter() - t0)
     e2e = n * e2e_steps * ws / t_e2e
-
-    extra = {}
-    if not args.no_accuracy:
-        f32, e32, _ = sysm.forces(energy=True)
-        pos_now, vel_now = sysm.state()
-        with ex.MidpointLJ(case["boxes"], case["natoms"], precision="fp64", device=lr, **lj) as s64:
-            s64.set_atoms(pos_now, case["types"], vel_now)
-            f64, e64, _ = s64.forces(energy=True)
-            err = np.sqrt(((f32 - f64) ** 2).sum(1))
-            fr = np.sqrt((f64 * f64).sum(1).mean())
-            s64.run(4, dt)
-            k64 = 10
-            o64 = s64.run(k64, dt)
-            v64 = n * k64 / (o64["ms"] * 1e-3)
-            d64 = s64.run(drift_steps, dt, graph_chunk=50, energies=True)
-        dm = sysm.run(drift_steps, dt, graph_chunk=50, energies=True)
-        em = dm["ekin"] + dm["epot"]
-        e6 = d64["ekin"] + d64["epot"]
-        drift_m = [drift_per_1000(em[:, b]) for b in range(nboxes)]
-        drift_d = [drift_per_1000(e6[:, b]) for b in range(nboxes)]
-        extra = {"fp64": {"value": v64, "ms_per_step": o64["ms"] / k64},
-                 "mixed_over_fp64": value / ws / v64,
-                 "force_rel_err_vs_fp64": {"rms": float(np.sqrt((err * err).mean()) / fr),
-                                           "max": float(err.max() / fr)},
-                 "epot_rel_err_vs_fp64": float(np.abs(e32.sum() - e64.sum()) / abs(e64.sum())),
-                 "energy_drift_per_1000_steps": {"mixed": drift_m[0], "fp64": drift_d[0], "steps": drift_steps}}
-        if nboxes > 1:
-            # a box's total energy can be near zero (gas-like boxes), which makes
-            # (E - E0)/|E0| meaningless there: also report (E - E0)/<Ekin>
-            km, k6 = dm["ekin"].mean(0), d64["ekin"].mean(0)
-            am, ad = np.abs(drift_m), np.abs(drift_d)
-            bm = np.abs([drift_per_1000(em[:, b], km[b]) for b in range(nboxes)])
-            bd = np.abs([drift_per_1000(e6[:, b], k6[b]) for b in range(nboxes)])
-            extra["energy_drift_per_1000_steps"] = {
-                "mixed": {"median_abs": float(np.median(am)), "max_abs": float(am.max()),
-                          "median_abs_vs_ekin": float(np.median(bm)), "max_abs_vs_ekin": float(bm.max())},
-                "fp64": {"median_abs": float(np.median(ad)), "max_abs": float(ad.max()),
-                         "median_abs_vs_ekin": float(np.median(bd)), "max_abs_vs_ekin": float(bd.max())},
-                "per_box": "per-box drift; median and max of |drift| over the boxes, relative to |E0| and "
-                           "to the box's mean kinetic energy", "steps": drift_steps}
+    phases = sysm.time_phases(10, dt)  # advances the state: last
+    sysm.close()
 
     line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": wsteps, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": label, "atoms": n, "boxes": nboxes, "rc": lj.get("rc"), "dt": dt,
-                       "precision": "mixed", "graph_chunk": chunk,
-                       "tile": list(tuning["tile"]) if isinstance(tuning["tile"], tuple) else tuning["tile"],
-                       "warps": tuning["warps"], "tile_balance": tuning["tile_balance"],
-                       "l2": "working set > L2 (per-step HBM traffic ~0.2 KB per atom)" if n * 200 > 129e6
-                       else "working set fits L2 (small configuration)",
-                       "parallelism": f"replicas{ws}"},
+            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": config_of(args.workload, case),
+            "precision": "mixed", "tuning": {**tune_info, "graph_chunk": chunk},
             "clocks": clk.summary(),
-            "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n},
-            # per step: kick+drift+bin count, 2 scan kernels, finalize, pair, redo pass
+            "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
+                    "call": "examd_gpu_forces_at (positions in, forces out, pinned host buffers)"},
+            # per step: kick+drift+bin count, 2 scan kernels, finalize, pair, redo pass; + the closing kick
             "gpu_launches": 6 * args.steps + 1,
+            "phases_ms_per_step": phases,
             # pair rates of the timed run (the counters of one force evaluation x steps / time)
             "pairs": {"interactions_per_s": cnt["accepted"] * args.steps * ws / (t_ms * 1e-3),
                       "candidates_per_s": cnt["candidates"] * args.steps * ws / (t_ms * 1e-3),
                       "kernel_interactions_per_s": cnt["accepted"] / (k_ms * 1e-3)},
             "roofline": {"bound": "fp32", "kernel": "k_pair (mixed)", "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                         "traffic": traffic, "kernel_ms": k_ms, "flops_per_launch": flops,
-                         "candidates": cnt["candidates"], "accepted": cnt["accepted"],
-                         "peak_source": peak_src},
-            **extra}
-    if rk == 0 and not args.no_cpu and args.workload == "liquid":
-        line["cpu_baseline"] = cpu_baseline(state, case["boxes"][0, 0])
+                         "traffic": traffic, "traffic_source": traffic_src, "kernel_ms": k_ms,
+                         "flops_per_launch": flops, "candidates": cnt["candidates"], "accepted": cnt["accepted"],
+                         "peak_source": peak_src}}
+    if ws == 1 and not args.no_accuracy:
+        line.update(accuracy_and_drift(ex, case, w, lj, tuning, lr, dt))
+    if rk == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(case)
     if rk == 0:
         print(json.dumps(line), flush=True)
-    sysm.close()
     barrier(dist)
 
 

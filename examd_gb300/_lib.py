@@ -90,6 +90,8 @@ def load():
             "examd_gpu_forces": (C.c_int, [ctxp, dp, dp, dp, C.c_int]),
             "examd_gpu_forces_at": (C.c_int, [ctxp, dp, dp, dp, dp, C.c_int]),
             "examd_gpu_run": (C.c_int, [ctxp, C.c_int, C.c_double, C.c_int, dp, C.POINTER(Stats)]),
+            "examd_gpu_prepare_run": (C.c_int, [ctxp, C.c_double, C.c_int, C.c_int]),
+            "examd_gpu_time_phases": (C.c_int, [ctxp, C.c_int, C.c_double, dp]),
             "examd_gpu_get_state": (C.c_int, [ctxp, dp, dp]),
             "examd_gpu_kinetic": (C.c_int, [ctxp, dp]),
             "examd_kinetic_static": (C.c_int, [C.c_int, C.c_int64, C.c_int, i64p, vp, vp, vp, vp, C.c_int, dp, dp,

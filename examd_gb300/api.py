@@ -224,6 +224,19 @@ class MidpointLJ:
             out["epot"] = en[:nsteps, :, 1].copy()
         return out
 
+    def prepare_run(self, dt, graph_chunk, energies=False):
+        """Capture the step-loop graph that run(nsteps, dt, graph_chunk, energies)
+        replays, without running a step (keeps capture out of a timed run)."""
+        self._chk(self._lib.examd_gpu_prepare_run(self._ctx, float(dt), int(graph_chunk), 1 if energies else 0),
+                  "examd_gpu_prepare_run")
+
+    def time_phases(self, nsteps, dt):
+        """Average device ms per step of (kick + drift + binning count, scan + scatter, pair kernels) over
+        nsteps eager steps; advances the state (timing only)."""
+        ms = np.zeros(3)
+        self._chk(self._lib.examd_gpu_time_phases(self._ctx, int(nsteps), float(dt), _d(ms)), "examd_gpu_time_phases")
+        return {"kick_bin_count": float(ms[0]), "bin_scan_scatter": float(ms[1]), "pair": float(ms[2])}
+
     def state(self):
         pos = np.zeros((self.n, 3))
         vel = np.zeros((self.n, 3))

@@ -1234,6 +1234,43 @@ int ensure_ebuf(examd_ctx* ctx, int steps) {
   return EXAMD_OK;
 }
 
+// The steady-state step loop of `chunk` steps (merged kicks) as one CUDA
+// graph for buffer parity `parity`, captured and instantiated unless the
+// cached one already matches.  Captures only: no step runs.
+int ensure_chunk_graph(examd_ctx* ctx, int chunk, double dt, bool wantE, int parity) {
+  const bool rebuild = !ctx->gexec || ctx->g_parity != parity || ctx->g_chunk != chunk ||
+                       ctx->g_energy != (int)wantE || ctx->g_dt != dt || ctx->g_cap != ctx->cap;
+  if (!rebuild) return EXAMD_OK;
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  ctx->gexec = nullptr;
+  const int nb = ctx->nboxes;
+  const int saved = ctx->cur;
+  ctx->cur = parity;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+  int src = EXAMD_OK;
+  for (int j = 0; j < chunk && src == EXAMD_OK; ++j)
+    src = step_once(ctx, dt, dt, wantE ? ctx->boxKE + (size_t)j * nb : nullptr,
+                    wantE ? ctx->boxE + (size_t)j * nb : nullptr, wantE ? ctx->boxW + (size_t)j * nb : nullptr);
+  cudaError_t ce = cudaStreamEndCapture(ctx->st, &g);
+  // capture advanced the host-side parity; the graph leaves it unchanged (chunk even)
+  ctx->cur = saved;
+  if (src != EXAMD_OK) return src;
+  if (ce != cudaSuccess) return ctx->cuda_fail(ce, "cudaStreamEndCapture");
+  ce = cudaGraphInstantiate(&ctx->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) {
+    ctx->gexec = nullptr;
+    return ctx->cuda_fail(ce, "cudaGraphInstantiate");
+  }
+  ctx->g_parity = parity;
+  ctx->g_chunk = chunk;
+  ctx->g_energy = wantE;
+  ctx->g_dt = dt;
+  ctx->g_cap = ctx->cap;
+  return EXAMD_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1269,32 +1306,8 @@ int examd_gpu_run(examd_ctx* ctx, int nsteps, double dt, int graph_chunk, double
   while (done < nsteps) {
     const int left = nsteps - done;
     if (chunk > 0 && left >= chunk) {
-      const bool rebuild = !ctx->gexec || ctx->g_parity != ctx->cur || ctx->g_chunk != chunk ||
-                           ctx->g_energy != (int)wantE || ctx->g_dt != dt || ctx->g_cap != ctx->cap;
-      if (rebuild) {
-        if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
-        ctx->gexec = nullptr;
-        const int parity = ctx->cur;
-        cudaGraph_t g;
-        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        int src = EXAMD_OK;
-        for (int j = 0; j < chunk && src == EXAMD_OK; ++j)
-          src = step_once(ctx, dt, dt, wantE ? ctx->boxKE + (size_t)j * nb : nullptr,
-                          wantE ? ctx->boxE + (size_t)j * nb : nullptr, wantE ? ctx->boxW + (size_t)j * nb : nullptr);
-        cudaError_t ce = cudaStreamEndCapture(st, &g);
-        if (src != EXAMD_OK) return src;
-        if (ce != cudaSuccess) return ctx->cuda_fail(ce, "cudaStreamEndCapture");
-        ce = cudaGraphInstantiate(&ctx->gexec, g, 0);
-        cudaGraphDestroy(g);
-        if (ce != cudaSuccess) return ctx->cuda_fail(ce, "cudaGraphInstantiate");
-        // capture advanced the host-side parity; the graph leaves it unchanged (chunk even)
-        ctx->cur = parity;
-        ctx->g_parity = parity;
-        ctx->g_chunk = chunk;
-        ctx->g_energy = wantE;
-        ctx->g_dt = dt;
-        ctx->g_cap = ctx->cap;
-      }
+      rc = ensure_chunk_graph(ctx, chunk, dt, wantE, ctx->cur);
+      if (rc) return rc;
       CK(cudaGraphLaunch(ctx->gexec, st));
       if (wantE) {
         // slot j: ekin at the start of local step j (= after global step done + j), epot after it
@@ -1355,6 +1368,67 @@ int examd_gpu_run(examd_ctx* ctx, int nsteps, double dt, int graph_chunk, double
       }
     }
   }
+  return EXAMD_OK;
+}
+
+int examd_gpu_prepare_run(examd_ctx* ctx, double dt, int graph_chunk, int energies) {
+  if (!ctx || !(dt > 0) || graph_chunk < 0) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  const int chunk = graph_chunk > 0 ? (graph_chunk + 1) / 2 * 2 : 0;
+  int rc = ensure_ebuf(ctx, std::max(chunk, 1) + 1);
+  if (rc) return rc;
+  if (!ctx->forces_valid) {
+    rc = run_pair(ctx, false, false);
+    if (rc) return rc;
+    rc = check_status(ctx);
+    if (rc) return rc;
+    ctx->forces_valid = true;
+  }
+  if (chunk == 0) return EXAMD_OK;
+  // the run's first step flips the sort's double buffer: its graph chunks
+  // run at the other parity
+  rc = ensure_chunk_graph(ctx, chunk, dt, energies != 0, 1 - ctx->cur);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->st));
+  return EXAMD_OK;
+}
+
+int examd_gpu_time_phases(examd_ctx* ctx, int nsteps, double dt, double* ms) {
+  if (!ctx || nsteps < 1 || !(dt > 0) || !ms) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  cudaStream_t st = ctx->st;
+  int rc;
+  if (!ctx->forces_valid) {
+    rc = run_pair(ctx, false, false);
+    if (rc) return rc;
+    ctx->forces_valid = true;
+  }
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < nsteps; ++k) {
+    // one steady-state step (merged kick), as the captured loop runs it
+    CK(cudaEventRecord(ctx->e0, st));
+    CK(launch_kick(kick_args(ctx, dt, dt, true, 0.0, nullptr), st));
+    CK(cudaEventRecord(ctx->e1, st));
+    rc = finish_binning(ctx, false);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->e2, st));
+    rc = run_pair(ctx, false, false);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->e3, st));
+    CK(cudaStreamSynchronize(st));
+    float t01 = 0.f, t12 = 0.f, t23 = 0.f;
+    CK(cudaEventElapsedTime(&t01, ctx->e0, ctx->e1));
+    CK(cudaEventElapsedTime(&t12, ctx->e1, ctx->e2));
+    CK(cudaEventElapsedTime(&t23, ctx->e2, ctx->e3));
+    acc[0] += t01;
+    acc[1] += t12;
+    acc[2] += t23;
+  }
+  rc = check_status(ctx);
+  if (rc) return rc;
+  for (int a = 0; a < 3; ++a) ms[a] = acc[a] / nsteps;
   return EXAMD_OK;
 }
 

@@ -149,6 +149,25 @@ int examd_gpu_forces_at(examd_ctx *ctx, const double *pos, double *forces,
 int examd_gpu_run(examd_ctx *ctx, int nsteps, double dt, int graph_chunk,
                   double *energies, examd_stats *stats);
 
+/* Capture, without running any step, the CUDA graph that the next
+ * examd_gpu_run(ctx, nsteps, dt, graph_chunk, energies ? buf : NULL, ...)
+ * replays, so that the capture and instantiation stay out of a timed run (the
+ * reference times its force call alone, exaMD.f90:241-253).  Also sizes the
+ * per-step energy buffers and computes the forces at the current positions
+ * if none are held.  A no-op for graph_chunk = 0. */
+int examd_gpu_prepare_run(examd_ctx *ctx, double dt, int graph_chunk,
+                          int energies);
+
+/* Device time of the step's phases, averaged over nsteps eager steps of size
+ * dt: ms[0] the kick with drift, wrap and binning count; ms[1] the rest of
+ * the binning (scan and scatter); ms[2] the pair kernel and the mixed form's
+ * redo pass.  CUDA events on the context's stream around each phase (the
+ * reference stamps its force call with MPI_WTIME, exaMD.f90:234-263).  The
+ * steps use the merged kick of the captured loop (v += dt F/m), so they
+ * advance the state but are not a velocity-Verlet trajectory from a state
+ * that examd_gpu_run left at full step: for timing only. */
+int examd_gpu_time_phases(examd_ctx *ctx, int nsteps, double dt, double *ms);
+
 /* Current positions and velocities in the caller's order (3*n each, NULL to
  * skip). */
 int examd_gpu_get_state(examd_ctx *ctx, double *pos, double *vel);

@@ -1,5 +1,5 @@
-"""Size-independent properties at the benchmark sizes, where the CPU oracle is
-too slow to compare atom by atom:
+"""Size-independent properties at the benchmark sizes (the atom-by-atom
+comparison with the oracle at these sizes is in test_gpu_configs_vs_oracle.py):
 
 - Newton's third law: the forces of each box sum to (nearly) zero;
 - permutation invariance: forces follow the atoms (bit for bit in the mixed
