@@ -184,14 +184,16 @@ class ClockSampler:
 
 def read_traffic(workload):
     """DRAM bytes per pair-kernel launch from the committed ncu summary of this workload, if any."""
-    names = {"mixture": "pair_mixed_mixture_16777216.md", "liquid": "pair_mixed_fcc64_1048576.md"}
+    names = {"mixture": ("pair_mixed_mixture_2097152.md", "traffic_bytes_per_launch_16777216"),
+             "liquid": ("pair_mixed_fcc64_1048576.md", "traffic_bytes_per_launch")}
     if workload not in names:
         return None, None
-    p = os.path.join(ROOT, "profiles", names[workload])
+    fname, key = names[workload]
+    p = os.path.join(ROOT, "profiles", fname)
     if not os.path.exists(p):
         return None, None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
-    return (float(m.group(1)), f"profiles/{names[workload]}") if m else (None, None)
+    m = re.search(key + r":\s*([0-9.eE+]+)", open(p).read())
+    return (float(m.group(1)), f"profiles/{fname} ({key})") if m else (None, None)
 
 
 def fp32_peak():
