@@ -333,7 +333,8 @@ def accuracy_and_drift(ex, case, w, lj, tuning, lr, dt):
         s.prepare_run(dt, 10)
         o32 = s.run(20, dt, graph_chunk=10)
     t64 = ex.autotune(boxes, natoms, pos_eq, types, precision="fp64", device=lr, **lj)
-    tune64 = {"tile": t64["tile"], "warps": t64["warps"], "tile_balance": t64["tile_balance"]}
+    tune64 = {"tile": t64["tile"], "warps": t64["warps"], "tile_balance": t64["tile_balance"],
+              "block_length": t64["block_length"]}
     with ex.MidpointLJ(boxes, natoms, precision="fp64", device=lr, **tune64, **lj) as s64:
         s64.set_atoms(pos_eq, types, vel_eq)
         f64, e64, _ = s64.forces(energy=True)
@@ -352,7 +353,8 @@ def accuracy_and_drift(ex, case, w, lj, tuning, lr, dt):
     drift_m = [drift_per_1000(em[:, b]) for b in range(nboxes)]
     drift_d = [drift_per_1000(e6[:, b]) for b in range(nboxes)]
     out = {"fp64": {"value": v64, "ms_per_step": o64["ms"] / k64, "tile": list(tune64["tile"]),
-                    "warps": tune64["warps"], "tile_balance": tune64["tile_balance"], "graph_chunk": 10,
+                    "warps": tune64["warps"], "tile_balance": tune64["tile_balance"],
+                    "cell_edge": tune64["block_length"] or "rc/2 (the reference's)", "graph_chunk": 10,
                     "state": "equilibrated"},
            "mixed_equilibrated": {"value": v32, "ms_per_step": o32["ms"] / 20, "graph_chunk": 10},
            "mixed_over_fp64": v32 / v64,
@@ -414,8 +416,10 @@ def main():
         # tile shape, warps per CTA and tile split for these atoms (examd_autotune)
         t = ex.autotune(case["boxes"], case["natoms"], case["pos"], case["types"], precision="mixed", device=lr,
                         **lj)
-        tuning = {"tile": t["tile"], "warps": t["warps"], "tile_balance": t["tile_balance"]}
-        tune_info = {"tile": list(t["tile"]), "warps": t["warps"], "tile_balance": t["tile_balance"]}
+        tuning = {"tile": t["tile"], "warps": t["warps"], "tile_balance": t["tile_balance"],
+                  "block_length": t["block_length"]}
+        tune_info = {"tile": list(t["tile"]), "warps": t["warps"], "tile_balance": t["tile_balance"],
+                     "cell_edge": t["block_length"] or "rc/2 (the reference's)"}
     sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **tuning, **lj)
     sysm.set_atoms(case["pos"], case["types"], case["vel"])
     sysm.run(args.warmup, dt)  # exactly W untimed steps
@@ -429,8 +433,14 @@ def main():
     t_ms = allmax(dist, out["ms"])
     value = n * args.steps * ws / (t_ms * 1e-3)
 
-    # pair-kernel roofline: algorithmic FLOPs per launch / event-timed duration
+    # pair-kernel roofline: algorithmic FLOPs per launch / event-timed duration.  The candidates are the
+    # reference's pair calls at its own cell edge rc/2 (exaMD.f90:56), whatever edge the autotuner picked
     cnt = sysm.counters()
+    if tuning.get("block_length"):
+        pos_now, _ = sysm.state()
+        with ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **lj) as s0:
+            s0.set_atoms(pos_now, case["types"])
+            cnt["candidates"] = s0.counters()["candidates"]
     flops = 8.0 * cnt["candidates"] + 22.0 * cnt["accepted"]
     peak, peak_src = fp32_peak()
     _, k_ms = sysm.time_forces(20)

@@ -94,10 +94,11 @@ def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, 
 
 
 def autotune(boxes, natoms, pos, types=None, cache=None, **kw):
-    """Tile shape, warps per CTA and tile split for this system, picked by
-    timing the pair kernel on these atoms (examd_autotune).  cache: path of a
-    text cache of earlier choices, or None.  Returns dict(tile, warps,
-    tile_balance, ms per launch)."""
+    """Cell edge, tile shape, warps per CTA and tile split for this system,
+    picked by timing the pair kernel on these atoms (examd_autotune).  cache:
+    path of a text cache of earlier choices, or None.  Returns dict(tile,
+    warps, tile_balance, block_length (None: the reference's rc/2), ms per
+    launch); the first four are MidpointLJ keyword arguments."""
     lib, p, arr, b, n, _ = _setup(boxes, natoms, **kw)
     pp = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
     t = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
@@ -107,7 +108,8 @@ def autotune(boxes, natoms, pos, types=None, cache=None, **kw):
     check(lib.examd_autotune(C.byref(p), len(n), arr, len(pp), _d(pp), _i(t), path, C.byref(best), C.byref(ms)),
           "examd_autotune")
     return {"tile": tuple(int(v) for v in best.tile), "warps": int(best.warps),
-            "tile_balance": int(best.tile_balance), "ms": ms.value}
+            "tile_balance": int(best.tile_balance),
+            "block_length": float(best.cell_edge) if best.cell_edge > 0 else None, "ms": ms.value}
 
 
 class MidpointLJ:
@@ -148,7 +150,8 @@ class MidpointLJ:
     def tuned(cls, boxes, natoms, pos, types=None, vel=None, cache=None, **kw):
         """A system whose tile shape, CTA width and tile split the autotuner picked for these atoms."""
         r = autotune(boxes, natoms, pos, types, cache, **kw)
-        kw = dict(kw, tile=r["tile"], warps=r["warps"], tile_balance=r["tile_balance"])
+        kw = dict(kw, tile=r["tile"], warps=r["warps"], tile_balance=r["tile_balance"],
+                  block_length=r["block_length"])
         s = cls(boxes, natoms, **kw)
         s.set_atoms(pos, types, vel)
         s.tuning = r

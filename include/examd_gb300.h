@@ -210,11 +210,14 @@ int examd_kinetic_static(int device, int64_t natoms, int nboxes,
 int examd_gpu_scale_velocities(examd_ctx *ctx, const double *factor);
 
 /* Autotuner (no counterpart in the reference, whose decomposition is the
- * METIS partition): time the pair kernel on these atoms for tile shapes of 3-6
- * home cells per axis, 4 or 8 warps per CTA and, where a box has a last cell
- * of about 1.5 edges or more, both tile splits (tile_balance), and return the
- * fastest in *best (a copy of *params with tile, warps and tile_balance set)
- * and its time per launch in *best_ms.
+ * METIS partition and whose block edge is a parameter, SRC/exaMD_utils.f90:
+ * 167-190, set to rc/2 by the driver, exaMD.f90:56): time the pair kernel on
+ * these atoms for tile shapes of 3-6 home cells per axis, 4 or 8 warps per
+ * CTA and, where a box has a last cell of about 1.5 edges or more, both tile
+ * splits (tile_balance); then the cell edge at 1.1 and 1.2 times the
+ * caller's (rc/2 by default) with the four fastest of those.  Returns the
+ * fastest in *best (a copy of *params with tile, warps, tile_balance and
+ * cell_edge set) and its time per launch in *best_ms.
  * cache_path (may be NULL): a text file of earlier choices keyed by device,
  * precision, types, cutoff, box count, atom count and density; a hit returns
  * without timing, a miss is appended.  pos/type as in examd_gpu_set_atoms. */

@@ -297,3 +297,34 @@ def test_empty_and_single_atom(gpulib):
         s.set_atoms(np.zeros((0, 3)))
         f, ep, _ = s.forces(energy=True)
         assert f.shape == (0, 3) and ep[0] == 0
+
+
+@pytest.mark.parametrize("edge", [1.375, 1.5])
+def test_fp64_matches_oracle_at_larger_cell_edges(gpulib, oracle, edge):
+    """A cell edge above rc/2 (the autotuner tries 1.1 and 1.2 x rc/2): the
+    reference's block rule and 63-entry table at that block length
+    (exaMD_domain_create takes it as a parameter, SRC/exaMD_utils.f90:167-190),
+    against the oracle at the same length: forces, energy, virial and the
+    candidate and accepted pair counts.  Both edges have few significant bits,
+    so the library uses them as given."""
+    L = np.array([16.0, 17.0, 18.0])
+    pos = gas(gpulib, L, 3000, 0.8, 12)
+    ref = oracle.forces_typed(pos, L, 2.5, block_length=edge)
+    with gpulib.MidpointLJ(L, [len(pos)], precision="fp64", rc=2.5, block_length=edge) as s:
+        s.set_atoms(pos)
+        f, ep, w = s.forces(energy=True)
+        cnt = s.counters()
+    mx, _ = rel_err(f, ref["forces"])
+    assert mx <= TOL64
+    assert ep[0] == pytest.approx(ref["epot"], rel=TOL64)
+    assert w[0] == pytest.approx(ref["virial"], rel=TOL64)
+    assert cnt["candidates"] == ref["counts"].candidates
+    assert cnt["accepted"] == ref["counts"].accepted
+    # more candidates than at rc/2, the same accepted pairs
+    ref0 = oracle.forces_typed(pos, L, 2.5)
+    assert ref["counts"].candidates > ref0["counts"].candidates
+    assert ref["counts"].accepted == ref0["counts"].accepted
+    with gpulib.MidpointLJ(L, [len(pos)], precision="mixed", rc=2.5, block_length=edge) as s:
+        s.set_atoms(pos)
+        g, _, _ = s.forces()
+    assert rel_err(g, ref["forces"])[1] <= TOL_MIXED_RMS

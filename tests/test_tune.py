@@ -29,6 +29,7 @@ def test_tuned_choice_cached_and_equivalent(gpulib, tmp_path, precision, tol):
     t = sorted(r["tile"])
     assert t[0] in (3, 4, 5, 6) and t[2] - t[0] <= 2
     assert r["warps"] in (4, 8) and r["tile_balance"] in (0, 1) and r["ms"] > 0
+    assert r["block_length"] is None or 1.25 * 1.09 <= r["block_length"] <= 1.25 * 1.21
     assert len(cache.read_text().splitlines()) == 1
     r2 = gpulib.autotune(L, [len(pos)], pos, cache=cache, precision=precision, rc=2.5)
     assert r2 == r and len(cache.read_text().splitlines()) == 1  # a hit, no new timing
@@ -44,8 +45,8 @@ def test_tuned_choice_cached_and_equivalent(gpulib, tmp_path, precision, tol):
 
 def test_cache_hit_needs_no_device(gpulib, tmp_path):
     """A cached choice is returned without timing (so without a device): tile,
-    warps and tile split come from the cache line; entries written before the
-    tile split existed (five fields, no "|tb" key) are not used."""
+    warps, tile split and cell edge come from the cache line; entries written
+    before the cell edge was tuned (no "|ce" key) are not used."""
     from examd_gb300 import _lib
     L = np.array([107.49, 107.49, 107.49])
     n = 1048576
@@ -65,10 +66,10 @@ def test_cache_hit_needs_no_device(gpulib, tmp_path):
     rho = np.round(n / L.prod() * 20.0) / 20.0
     key = f"unknown|mixed|nt1|rc2.5|boxes1|n{lg:.2f}|rho{rho:.2f}"
     cache = tmp_path / "tune.txt"
-    cache.write_text(f"{key}|5 5 5 8 0.5\n"                 # old format: ignored
+    cache.write_text(f"{key}|5 5 5 8 0.5\n"                 # old formats: ignored
                      f"{key}|tb|6 6 6 8 0.41 1\n"
-                     f"{key}|tb|5 4 4 4 0.42 0\n"
-                     f"{key}|tb|6 6 5 8 0.40 1\n")          # the last entry wins
+                     f"{key}|ce|5 4 4 4 0.42 0 0\n"
+                     f"{key}|ce|6 6 5 8 0.40 1 1.375\n")    # the last entry wins
     best = _lib.Params()
     ms = C.c_double()
     pos = np.zeros((n, 3))
@@ -76,3 +77,4 @@ def test_cache_hit_needs_no_device(gpulib, tmp_path):
                                     os.fsencode(str(cache)), C.byref(best), C.byref(ms))
     assert rc == _lib.OK
     assert tuple(best.tile) == (6, 6, 5) and best.warps == 8 and best.tile_balance == 1 and ms.value == 0.40
+    assert best.cell_edge == 1.375
