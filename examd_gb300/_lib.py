@@ -11,6 +11,8 @@ import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libexamd_gb300.so")
+# the index-checked build (python -m examd_gb300.build --checked), loaded instead when EXAMD_CHECKED=1
+LIB_CHECKED_PATH = os.path.join(HERE, "_lib", "libexamd_gb300_checked.so")
 
 MAX_TYPES = 4
 STATIC_MAX_ATOMS = 1048576  # EXAMD_STATIC_MAX_ATOMS
@@ -31,6 +33,7 @@ ERR_STATE = 208
 ERR_NO_DEVICE = 209
 ERR_IO = 210
 ERR_PAIRFN = 211
+ERR_CHECK = 212
 POT_LJ, POT_LJ_SHIFTED, POT_WCA = 0, 1, 2
 
 
@@ -72,11 +75,13 @@ def load():
     with _lock:
         if _lib is not None:
             return _lib
-        if not os.path.exists(LIB_PATH):
+        checked = os.environ.get("EXAMD_CHECKED") == "1"
+        path = LIB_CHECKED_PATH if checked else LIB_PATH
+        if not os.path.exists(path):
             raise FileNotFoundError(
-                f"{LIB_PATH} is missing: build it with `python -m examd_gb300.build` "
+                f"{path} is missing: build it with `python -m examd_gb300.build{' --checked' if checked else ''}` "
                 "(or __graft_entry__.build()); there is no CPU fallback")
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         dp = C.POINTER(C.c_double)
         ip = C.POINTER(C.c_int)
         i64p = C.POINTER(C.c_int64)

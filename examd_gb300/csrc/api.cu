@@ -297,6 +297,7 @@ int status_to_code(int st) {
   if (st & ST_OUTSIDE) return EXAMD_ERR_OUTSIDE;
   if (st & ST_OVERFLOW) return EXAMD_ERR_CELL_OVERFLOW;
   if (st & ST_TIMEOUT) return EXAMD_ERR_TIMEOUT;
+  if (st & ST_BOUNDS) return EXAMD_ERR_CHECK;
   return EXAMD_OK;
 }
 
@@ -359,6 +360,7 @@ const char* examd_gpu_strerror(int code) {
     case EXAMD_ERR_NO_DEVICE: return "no usable sm_103 CUDA device";
     case EXAMD_ERR_IO: return "file missing, unreadable or malformed";
     case EXAMD_ERR_PAIRFN: return "the pair function returned an error (e.g. coincident atoms)";
+    case EXAMD_ERR_CHECK: return "an index check of the checked build failed";
     default: return "unknown status";
   }
 }
@@ -804,7 +806,7 @@ int finish_binning(examd_ctx* ctx, bool want_inv) {
                                               ctx->V[s][1], ctx->V[s][2], ctx->meta[s], ctx->id[s],
                                               ctx->X[d][0], ctx->X[d][1], ctx->X[d][2], ctx->V[d][0],
                                               ctx->V[d][1], ctx->V[d][2], ctx->meta[d], ctx->id[d], ctx->U,
-                                              ctx->cellS, want_inv ? ctx->inv : nullptr);
+                                              ctx->cellS, want_inv ? ctx->inv : nullptr, ctx->NC, ctx->status);
   }
   CK(cudaGetLastError());
   ctx->cur = d;
@@ -952,6 +954,8 @@ StepArgs step_args(examd_ctx* ctx) {
   s.P = ctx->P;
   s.N = ctx->N;
   s.fp64 = ctx->pc.fp64;
+  s.nc = ctx->NC;
+  s.status = ctx->status;
   return s;
 }
 

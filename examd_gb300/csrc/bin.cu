@@ -25,7 +25,7 @@ __device__ __forceinline__ void bin_one(int s, double x, double y, double z, int
   }
   const int gc = cell_of(x, y, z, B);
   cellOld[s] = gc;
-  slot[s] = atomicAdd(&count[gc], 1);
+  slot[s] = atomicAdd(&count[EXAMD_IDX(gc, B.cell0 + B.nb[0] * B.nb[1] * B.nb[2], status)], 1);
 }
 
 // Load caller-order AoS positions (and velocities) into the SoA master arrays,
@@ -177,11 +177,11 @@ __global__ void k_finalize(int64_t n, const int* __restrict__ cellOld, const int
                            double* __restrict__ Y1, double* __restrict__ Y2, double* __restrict__ W0,
                            double* __restrict__ W1, double* __restrict__ W2, int* __restrict__ meta2,
                            int* __restrict__ id2, float4* __restrict__ U, int* __restrict__ cellS,
-                           int* __restrict__ inv) {
+                           int* __restrict__ inv, int nc, int* __restrict__ status) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const int c = cellOld[s];
-  const int d = cstart[c] + slot[s];
+  const int c = (int)EXAMD_IDX(cellOld[s], nc, status);
+  const int d = (int)EXAMD_IDX(cstart[c] + slot[s], n, status);
   const int myid = id[s], mt = meta[s];
   double x = X0[s], y = X1[s], z = X2[s];
   Y0[d] = x;
@@ -201,7 +201,7 @@ __global__ void k_finalize(int64_t n, const int* __restrict__ cellOld, const int
   u.w = __int_as_float(mt & 0xff);
   U[d] = u;
   cellS[d] = c;
-  if (inv) inv[myid] = d;  // caller index -> sorted slot, when the caller's order is needed next
+  if (inv) inv[EXAMD_IDX(myid, n, status)] = d;  // caller index -> sorted slot, when the caller's order is needed next
 }
 
 // inv[id[s]] = s: the caller-order map of the current sorted order.

@@ -33,7 +33,43 @@ enum StatusBits : int {
   ST_OUTSIDE = 4,    // position outside [0,L) in strict mode
   ST_TIMEOUT = 8,    // a bounded wait gave up
   ST_PAIRFN = 16,    // the pair function returned an error
+  ST_BOUNDS = 32,    // checked build: an index check failed (the access went to index 0)
 };
+
+// Index-checked arrays of the checked build (-DEXAMD_CHECKED, the
+// counterpart of a memory checker on a pool where none may run): every
+// subscript is tested against the array's length; an index outside it sets
+// ST_BOUNDS in the status word and reads or writes element 0 instead, so the
+// kernel records the fault and finishes without touching memory outside its
+// buffers.  Without EXAMD_CHECKED an array is its plain pointer and the
+// checks cost nothing.
+#ifdef EXAMD_CHECKED
+template <class T>
+struct ChkArr {
+  T* p;
+  long long n;
+  int* st;
+  __device__ __forceinline__ T& operator[](long long i) const {
+    if (i < 0 || i >= n) {
+      atomicOr(st, ST_BOUNDS);
+      i = 0;
+    }
+    return p[i];
+  }
+};
+#define EXAMD_ARR(T, ptr, len, status) (examd::ChkArr<T>{(T*)(ptr), (long long)(len), (status)})
+#define EXAMD_IDX(i, len, status) examd::chk_index((i), (long long)(len), (status))
+__device__ __forceinline__ long long chk_index(long long i, long long n, int* st) {
+  if (i < 0 || i >= n) {
+    atomicOr(st, ST_BOUNDS);
+    return 0;
+  }
+  return i;
+}
+#else
+#define EXAMD_ARR(T, ptr, len, status) ((T*)(ptr))
+#define EXAMD_IDX(i, len, status) (i)
+#endif
 
 struct BoxDev {
   double L[3], Li[3];

@@ -20,7 +20,7 @@ __global__ void k_finalize(int64_t n, const int* cellOld, const int* slot, const
                            const double* X0, const double* X1, const double* X2, const double* V0,
                            const double* V1, const double* V2, const int* meta, const int* id, double* Y0,
                            double* Y1, double* Y2, double* W0, double* W1, double* W2, int* meta2, int* id2,
-                           float4* U, int* cellS, int* inv);
+                           float4* U, int* cellS, int* inv, int nc, int* status);
 constexpr int kScanTileHost = 2048;  // cells per scan block (kScanThreads * kScanItems)
 
 // ---- pair.cu ----------------------------------------------------------------
@@ -79,6 +79,8 @@ struct StepArgs {
   const void* P;
   int64_t N;
   bool fp64;
+  int nc;       // cells (the bmask length; index checks of the checked build)
+  int* status;  // the status word (index checks of the checked build)
 };
 
 // F = Fown + halo partials, in caller order, AoS doubles (out[3*id + a]); += if accumulate.

@@ -175,10 +175,9 @@ struct FixSum {
 // thermal configurations do not reach) is left out here and raises the
 // tile's flag (*big_flag); the redo pass adds it.  SIDE (the full redo pass):
 // such terms go to the FP32 side sums fr instead.
-template <bool MULTI, bool ENERGY, bool COUNT, bool SIDE>
-__device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, const int* qk, int* fa, float* fr,
-                                            int cap, const PairArgs& A, FixSum& ek, FixSum& wk, int& nacc,
-                                            int* big_flag) {
+template <bool MULTI, bool ENERGY, bool COUNT, bool SIDE, class QD, class FA, class FR>
+__device__ __forceinline__ void force_batch(int cnt, int qh, const QD& qd, FA& fa, FR& fr, int cap, const PairArgs& A,
+                                            FixSum& ek, FixSum& wk, int& nacc, int* big_flag) {
   const LJTable& lj = A.lj;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -261,11 +260,10 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const float4* qd, c
 // x_j - x_i plus the difference of the two staged copies' periodic images,
 // (n_j - n_i) L, which is exact (Sterbenz) and equals the reference's
 // dx - Nint(dx/L) L (SRC/exaMD_forces.f90:509-523); then user_func.f90:52-69.
-template <bool MULTI, bool ENERGY, bool COUNT>
-__device__ __forceinline__ void force_batch64(int cnt, const int* qk, const double* pd, const unsigned short* code,
-                                              const signed char* img, const double* Lbox, double* fd, int cap,
-                                              const LJTable& lj, double& esum, double& wsum, int* status,
-                                              int& nacc, int qh) {
+template <bool MULTI, bool ENERGY, bool COUNT, class QK, class PD, class CODE, class IMG, class FD>
+__device__ __forceinline__ void force_batch64(int cnt, const QK& qk, const PD& pd, const CODE& code, const IMG& img,
+                                              const double* Lbox, FD& fd, int cap, const LJTable& lj, double& esum,
+                                              double& wsum, int* status, int& nacc, int qh) {
   const int lane = threadIdx.x & 31;
   if (lane >= cnt) return;
   const unsigned key = (unsigned)qk[(qh + lane) & (kQueue - 1)];
@@ -325,20 +323,23 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   const int NE = EX * EY * EZ;
   const int cap = MODE == kMain ? A.cap : A.cap_redo;
   const Layout L = make_layout(FP64, cap, A.ne_max, A.ext_max, nw, MODE, PACK);
-  unsigned short* lstart = (unsigned short*)(smem + L.lstart);
-  int* gfirst = (int*)(smem + L.gfirst);
-  float* ox = (float*)(smem + L.ox);
-  float* oy = (float*)(smem + L.oy);
-  float* oz = (float*)(smem + L.oz);
-  float2* dyt = (float2*)(smem + L.dyt);
-  float2* dzt = (float2*)(smem + L.dzt);
-  signed char* img = (signed char*)(smem + L.img);
+  // shared-memory arrays (index-checked in the checked build)
+  int* const st = A.status;
+  auto lstart = EXAMD_ARR(unsigned short, smem + L.lstart, A.ne_max + 1, st);
+  auto gfirst = EXAMD_ARR(int, smem + L.gfirst, A.ne_max, st);
+  auto ox = EXAMD_ARR(float, smem + L.ox, A.ext_max + 1, st);
+  auto oy = EXAMD_ARR(float, smem + L.oy, A.ext_max + 1, st);
+  auto oz = EXAMD_ARR(float, smem + L.oz, A.ext_max + 1, st);
+  auto dyt = EXAMD_ARR(float2, smem + L.dyt, A.ext_max * kDT, st);
+  auto dzt = EXAMD_ARR(float2, smem + L.dzt, A.ext_max * kDT, st);
+  auto img = EXAMD_ARR(signed char, smem + L.img, FP64 ? 96 : 1, st);
   double* red = (double*)(smem + L.queue);  // scan and reduction scratch, before and after the queues' use
   int* cw = (int*)(smem + L.cw);
   OwnLut* sown = (OwnLut*)(smem + L.lut);
   const signed char* srows = &sown->rows[0][0];
-  float4* pf = (float4*)(smem + L.pf);
-  unsigned short* code = (unsigned short*)(smem + L.code);
+  auto pf = EXAMD_ARR(float4, smem + L.pf, cap, st);
+  auto code = EXAMD_ARR(unsigned short, smem + L.code, cap, st);
+  auto U = EXAMD_ARR(const float4, A.U, A.N, st);
 
   // (1) ext cells: global cell, count, first atom; ownership tables to smem
   for (int e = tid; e < NE; e += blockDim.x) {
@@ -386,7 +387,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         if (l < E) {
           if (FP64) img[32 * a + l] = (signed char)n;
           if (a > 0) {
-            float2* dt = a == 1 ? dyt : dzt;
+            auto dt = a == 1 ? dyt : dzt;
 #pragma unroll
             for (int d = -2; d <= 3; ++d) {
               const int l2 = l + d, ln = l + d + (d < 0);
@@ -452,22 +453,22 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     return;
   }
   // (3) stage atoms, one thread per ext cell
-  int* fa = (int*)(smem + L.fa);
-  float* fr = (float*)(smem + L.fr);  // redo pass: FP32 sums of the large terms
-  double* fd = (double*)(smem + L.fa);
-  double* pd = (double*)(smem + L.px);
+  auto fa = EXAMD_ARR(int, smem + L.fa, 3 * cap, st);
+  auto fr = EXAMD_ARR(float, smem + L.fr, 3 * cap, st);  // redo pass: FP32 sums of the large terms
+  auto fd = EXAMD_ARR(double, smem + L.fa, 3 * cap, st);
+  auto pd = EXAMD_ARR(double, smem + L.px, 3 * cap, st);
   for (int e = tid; e < NE; e += blockDim.x) {
     const int lx = e % EX, rr = e / EX, ly = rr % EY, lz = rr / EY;
     const int a0 = lstart[e], a1 = lstart[e + 1], g0 = gfirst[e];
     const unsigned short cc = (unsigned short)(lx | (ly << 5) | (lz << 10));
     for (int t = a0; t < a1; ++t) {
       const int g = g0 + (t - a0);
-      const float4 u = A.U[g];
+      const float4 u = U[g];
       if (FP64) {
         pf[t] = make_float4(ox[lx] + u.x, oy[ly] + u.y, oz[lz] + u.z, u.w);
-        pd[t] = A.X0[g];
-        pd[cap + t] = A.X1[g];
-        pd[2 * cap + t] = A.X2[g];
+        pd[t] = A.X0[EXAMD_IDX(g, A.N, st)];
+        pd[cap + t] = A.X1[EXAMD_IDX(g, A.N, st)];
+        pd[2 * cap + t] = A.X2[EXAMD_IDX(g, A.N, st)];
 #pragma unroll
         for (int c = 0; c < 3; ++c) fd[c * cap + t] = 0.0;
       } else {
@@ -496,20 +497,22 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   // per-warp queue of accepted pairs (mixed form: the separation and the key
   // in one 16-byte entry, r^2 recomputed from it; FP64 form: the key only)
   constexpr int kQe = FP64 ? 4 : 16;  // bytes per queue entry
-  float4* qd = (float4*)(smem + L.queue) + warp * kQueue;
-  int* qk = (int*)(smem + L.queue) + warp * kQueue;
+  auto qd = EXAMD_ARR(float4, (float4*)(smem + L.queue) + warp * kQueue, kQueue, st);
+  auto qk = EXAMD_ARR(int, (int*)(smem + L.queue) + warp * kQueue, kQueue, st);
   // per-warp tables (kWarpTab*): one step's items (ptA, ptB) and, mixed
   // form, the work unit's atoms (bt)
   unsigned char* wtab =
       smem + L.queue + kQe * kQueue * nw + warp * (FP64 ? kWarpTabFp64 : (PACK ? kWarpTabCompact : kWarpTabWide));
-  float4* ptA = (float4*)wtab;
-  void* ptB = wtab + 32 * 16;
-  float4* btA = (float4*)(wtab + (PACK ? 32 * 24 : 32 * 32));
-  void* btB = wtab + (PACK ? 32 * 40 : 32 * 48);
+  auto ptA = EXAMD_ARR(float4, wtab, 32, st);
+  auto ptB2 = EXAMD_ARR(int2, wtab + 32 * 16, 32, st);  // the compact layout's view
+  auto ptB4 = EXAMD_ARR(int4, wtab + 32 * 16, 32, st);  // the wide layout's view
+  auto btA = EXAMD_ARR(float4, wtab + (PACK ? 32 * 24 : 32 * 32), 32, st);
+  auto btB2 = EXAMD_ARR(int2, wtab + (PACK ? 32 * 40 : 32 * 48), 32, st);
+  auto btB4 = EXAMD_ARR(float4, wtab + (PACK ? 32 * 40 : 32 * 48), 32, st);
   int qn = 0, qh = 0;  // queued pairs and the ring's head
   const unsigned lt = (1u << lane) - 1u;
   const unsigned le = FULL >> (31 - lane);
-  unsigned char* r2l = smem + L.r2l + 64 * warp;  // FP64 form: two rank -> lane tables of 32
+  auto r2l = EXAMD_ARR(unsigned char, smem + L.r2l + 64 * warp, FP64 ? 64 : 1, st);  // FP64 form: two rank -> lane tables of 32
   // ---- accepted pairs go to the warp's queue (a ring of kQueue entries);
   // their forces are computed in full batches of 32 ----
   auto enqueue = [&](bool acc, const float4& dq, int key) {
@@ -528,7 +531,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
                                             qh);
       else
-        force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(32, qh, qd, qk, fa, fr, cap, A, ek, wk, nacc, big_flag);
+        force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(32, qh, qd, fa, fr, cap, A, ek, wk, nacc, big_flag);
       __syncwarp();
       qh = (qh + 32) & (kQueue - 1);
       qn -= 32;
@@ -583,9 +586,9 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int rk = __popc(hb & lt);
       ptA[rk] = make_float4(-pi.x, cy - pi.y, cz - pi.z, __int_as_float(MULTI ? i | (__float_as_int(pi.w) << 28) : i));
       if (PACK)
-        ((int2*)ptB)[rk] = make_int2(((lo1 - s0) & 0xffff) | ((lo2 - n1 - s0) << 16), s0 + n1);
+        ptB2[rk] = make_int2(((lo1 - s0) & 0xffff) | ((lo2 - n1 - s0) << 16), s0 + n1);
       else
-        ((int4*)ptB)[rk] = make_int4(lo1 - s0, s0 + n1, lo2 - n1 - s0, 0);
+        ptB4[rk] = make_int4(lo1 - s0, s0 + n1, lo2 - n1 - s0, 0);
     }
     __syncwarp();
     // distance tests; accepted pairs go to the queue
@@ -599,12 +602,12 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const float4 a = ptA[qr];
       int o1, e1, o2;
       if (PACK) {
-        const int2 b = ((const int2*)ptB)[qr];
+        const int2 b = ptB2[qr];
         o1 = (int)(short)(b.x & 0xffff);
         o2 = b.x >> 16;
         e1 = b.y;
       } else {
-        const int4 b = ((const int4*)ptB)[qr];
+        const int4 b = ptB4[qr];
         o1 = b.x;
         e1 = b.y;
         o2 = b.z;
@@ -753,10 +756,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
           const __half2 hm = __halves2half2(__float2half_rz(am2), __float2half_rz(am1));
           const __half2 hp = __halves2half2(__float2half_rz(ap1), __float2half_rz(ap2));
           btA[rk] = make_float4(apy, apz, *reinterpret_cast<const float*>(&hm), *reinterpret_cast<const float*>(&hp));
-          ((int2*)btB)[rk] = make_int2(wa, wc);
+          btB2[rk] = make_int2(wa, wc);
         } else {
           btA[rk] = make_float4(apy, apz, am2, am1);
-          ((float4*)btB)[rk] = make_float4(ap1, ap2, __int_as_float(wa), __int_as_float(wc));
+          btB4[rk] = make_float4(ap1, ap2, __int_as_float(wa), __int_as_float(wc));
         }
       }
       __syncwarp();
@@ -776,7 +779,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         if (PACK) {
           const float2 gm = __half22float2(*reinterpret_cast<const __half2*>(&b0v.z));
           const float2 gp = __half22float2(*reinterpret_cast<const __half2*>(&b0v.w));
-          const int2 b1v = ((const int2*)btB)[qr];
+          const int2 b1v = btB2[qr];
           xm2 = gm.x;
           xm1 = gm.y;
           xp1 = gp.x;
@@ -784,7 +787,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
           sq = b1v.x;
           cc = b1v.y;
         } else {
-          const float4 b1v = ((const float4*)btB)[qr];
+          const float4 b1v = btB4[qr];
           xm2 = b0v.z;
           xm1 = b0v.w;
           xp1 = b1v.x;
@@ -941,7 +944,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
                                           qh);
     else
-      force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(qn, qh, qd, qk, fa, fr, cap, A, ek, wk, nacc, big_flag);
+      force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(qn, qh, qd, fa, fr, cap, A, ek, wk, nacc, big_flag);
   }
   __syncthreads();
   // a large term was left out: list the tile for the redo pass
@@ -958,7 +961,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     if (FP64) {
       double* F = slot == 0 ? (double*)A.Fown : (double*)A.P + (size_t)(slot - 1) * 3 * A.N;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) F[c * A.N + g] = fd[c * cap + t];
+      for (int c = 0; c < 3; ++c) F[EXAMD_IDX(c * A.N + g, 3 * A.N, st)] = fd[c * cap + t];
     } else {
       float4* F = slot == 0 ? (float4*)A.Fown : (float4*)A.P + (size_t)(slot - 1) * A.N;
       if (MODE == kRedoBig) {
@@ -966,11 +969,12 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         // only (a copy's slot pattern is unique to one tile)
         const float x = fr[t], y = fr[cap + t], z = fr[2 * cap + t];
         if (x != 0.f || y != 0.f || z != 0.f) {
-          float4 v = F[g];
+          const int64_t gg = EXAMD_IDX(g, A.N, st);
+          float4 v = F[gg];
           v.x += x;
           v.y += y;
           v.z += z;
-          F[g] = v;
+          F[gg] = v;
         }
       } else {
         float f[3];
@@ -978,7 +982,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         for (int c = 0; c < 3; ++c)
           f[c] = MODE == kRedoFull ? fmaf((float)fa[c * cap + t], kFixInv, fr[c * cap + t])
                                    : (float)fa[c * cap + t] * kFixInv;
-        F[g] = make_float4(f[0], f[1], f[2], 0.f);
+        F[EXAMD_IDX(g, A.N, st)] = make_float4(f[0], f[1], f[2], 0.f);
       }
     }
   }

@@ -16,9 +16,9 @@ namespace examd {
 
 __device__ __forceinline__ void bin_store(int s, double x, double y, double z, const BoxDev& B,
                                           int* __restrict__ cellOld, int* __restrict__ slot,
-                                          int* __restrict__ count) {
+                                          int* __restrict__ count, int nc, int* status) {
   // same rule as bin.cu: exact cell of the FP64 position on the grid c * bl
-  const int gc = cell_of(x, y, z, B);
+  const int gc = (int)EXAMD_IDX(cell_of(x, y, z, B), nc, status);
   cellOld[s] = gc;
   slot[s] = atomicAdd(&count[gc], 1);
 }
@@ -26,7 +26,8 @@ __device__ __forceinline__ void bin_store(int s, double x, double y, double z, c
 // Sum of an atom's force partials: the owning tile's, then the halo slots in
 // increasing order (fixed order: deterministic).  Mixed form: Kahan in FP32.
 __device__ __forceinline__ void gather_force(const StepArgs& a, int64_t s, double f[3]) {
-  const int m = a.bmask[a.cellS[s]];
+  s = EXAMD_IDX(s, a.N, a.status);
+  const int m = a.bmask[EXAMD_IDX(a.cellS[s], a.nc, a.status)];
   if (a.fp64) {
     const double* Fo = (const double*)a.Fown;
     const double* P = (const double*)a.P;
@@ -239,7 +240,7 @@ __global__ void k_kick(const KickArgs k) {
       atomicOr(k.status, ST_NONFINITE);
       x[0] = x[1] = x[2] = 0.0;
     }
-    bin_store((int)s, x[0], x[1], x[2], B, k.cellOld, k.slot, k.count);
+    bin_store((int)s, x[0], x[1], x[2], B, k.cellOld, k.slot, k.count, k.s.nc, k.status);
   }
 }
 

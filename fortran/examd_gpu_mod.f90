@@ -36,6 +36,7 @@ Module examd_gpu_mod
   Integer(c_int), Parameter :: EXAMD_ERR_NO_DEVICE = 209
   Integer(c_int), Parameter :: EXAMD_ERR_IO = 210
   Integer(c_int), Parameter :: EXAMD_ERR_PAIRFN = 211
+  Integer(c_int), Parameter :: EXAMD_ERR_CHECK = 212
 
   Integer(c_int), Parameter :: EXAMD_MAX_TYPES = 4
   Integer(c_int), Parameter :: EXAMD_POT_LJ = 0, EXAMD_POT_LJ_SHIFTED = 1, EXAMD_POT_WCA = 2

@@ -46,6 +46,8 @@ extern "C" {
 #define EXAMD_ERR_NO_DEVICE 209     /* no CUDA device / wrong architecture    */
 #define EXAMD_ERR_IO 210            /* file missing, unreadable or malformed  */
 #define EXAMD_ERR_PAIRFN 211        /* the pair function returned an error    */
+#define EXAMD_ERR_CHECK 212         /* checked build (-DEXAMD_CHECKED): an index
+                                       of a kernel fell outside its array      */
 
 #define EXAMD_MAX_TYPES 4
 
