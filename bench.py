@@ -66,8 +66,10 @@ WORKLOADS = {
                  dt=0.005, eq=2000, every=20, settle=200, drift=500),
     "ensemble": dict(label="lj-ensemble-512-boxes-256-16384-rc2.5", gen="ensemble", args={"seed": 4},
                      dt=0.005, eq=2000, every=20, settle=200, drift=1000),
+    # the perfect lattice has zero forces: 100 NVE steps move the atoms off their sites before the force
+    # comparison (a relative error against F_rms = 0 would mean nothing)
     "fcc32k": dict(label="lj-fcc-32000-rho0.8442-T0.72-rc2.5", gen="fcc_lattice", args={"nc": 20, "seed": 1},
-                   dt=0.005, eq=0, every=0, settle=0, drift=1000),
+                   dt=0.005, eq=0, every=0, settle=100, drift=1000),
 }
 DEFAULT_WORKLOAD = "mixture"
 
