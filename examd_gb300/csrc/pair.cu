@@ -77,7 +77,7 @@ constexpr int kSeg = 4;                // lanes per segment of the i-side force 
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
-  int lstart, gfirst, ox, oy, oz, dyt, dzt, img, cw, r2l, lut, queue;
+  int lstart, gfirst, ox, oy, oz, dyt, dzt, img, cw, r2l, lut, ljt, queue;
   int pf, fa, px, code, fr;
   int bytes;
 };
@@ -114,6 +114,9 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.cw = o;     o = align16(o + 16);  // unit counter, large-term flag, staged-atom total
   L.r2l = o;    o = align16(o + (fp64 ? 64 * nw : 0));  // rank -> lane tables (FP64 form)
   L.lut = o;    o = align16(o + (int)sizeof(OwnLut));
+  // the LJ table per ordered type pair (several types): per-lane type indices
+  // would serialise on the kernel-parameter bank, shared memory serves them at once
+  L.ljt = o;    o = align16(o + (int)sizeof(LJ64) * EXAMD_MAX_TYPES * EXAMD_MAX_TYPES);
   const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64 : 16 * kQueue + (pack ? kWarpTabCompact : kWarpTabWide)) * nw;
   L.queue = o;  o = align16(o + qbytes);
   L.pf = o;     o = align16(o + 16 * cap);
@@ -177,7 +180,7 @@ struct FixSum {
 // such terms go to the FP32 side sums fr instead.
 template <bool MULTI, bool ENERGY, bool COUNT, bool SIDE, class QD, class FA, class FR>
 __device__ __forceinline__ void force_batch(int cnt, int qh, const QD& qd, FA& fa, FR& fr, int cap, const PairArgs& A,
-                                            FixSum& ek, FixSum& wk, int& nacc, int* big_flag) {
+                                            const LJ32* ljs, FixSum& ek, FixSum& wk, int& nacc, int* big_flag) {
   const LJTable& lj = A.lj;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -193,7 +196,7 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const QD& qd, FA& f
     i = key & 0x3fff;
     m = (key >> 14) & 0x3fff;
     LJ32 P = lj.p32[0];
-    if (MULTI) P = lj.p32[((key >> 28) & 3) * lj.nt + (key >> 30)];
+    if (MULTI) P = ljs[((key >> 28) & 3) * lj.nt + (key >> 30)];
     big = d.w < P.r2big;  // left to the redo pass
     float dg = 0.f, e = 0.f;
     const int rv = pair_fn32<ENERGY>(lj.pot, d.w, P, dg, e);
@@ -262,8 +265,9 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const QD& qd, FA& f
 // dx - Nint(dx/L) L (SRC/exaMD_forces.f90:509-523); then user_func.f90:52-69.
 template <bool MULTI, bool ENERGY, bool COUNT, class QK, class PD, class CODE, class IMG, class FD>
 __device__ __forceinline__ void force_batch64(int cnt, const QK& qk, const PD& pd, const CODE& code, const IMG& img,
-                                              const double* Lbox, FD& fd, int cap, const LJTable& lj, double& esum,
-                                              double& wsum, int* status, int& nacc, int qh) {
+                                              const double* Lbox, FD& fd, int cap, const LJTable& lj,
+                                              const LJ64* ljs, double& esum, double& wsum, int* status, int& nacc,
+                                              int qh) {
   const int lane = threadIdx.x & 31;
   if (lane >= cnt) return;
   const unsigned key = (unsigned)qk[(qh + lane) & (kQueue - 1)];
@@ -281,7 +285,7 @@ __device__ __forceinline__ void force_batch64(int cnt, const QK& qk, const PD& p
   if (nz) dz = __dadd_rn(dz, nz > 0 ? Lbox[2] : -Lbox[2]);
   const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
   LJ64 P = lj.p64[0];
-  if (MULTI) P = lj.p64[((key >> 28) & 3) * lj.nt + (key >> 30)];
+  if (MULTI) P = ljs[((key >> 28) & 3) * lj.nt + (key >> 30)];
   double dg = 0.0, e = 0.0;
   const int rv = pair_fn64<ENERGY>(lj.pot, d2, P, dg, e);
   if (rv == 0) {
@@ -337,6 +341,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   int* cw = (int*)(smem + L.cw);
   OwnLut* sown = (OwnLut*)(smem + L.lut);
   const signed char* srows = &sown->rows[0][0];
+  LJ32* ljs32 = (LJ32*)(smem + L.ljt);
+  LJ64* ljs64 = (LJ64*)(smem + L.ljt);
   auto pf = EXAMD_ARR(float4, smem + L.pf, cap, st);
   auto code = EXAMD_ARR(unsigned short, smem + L.code, cap, st);
   auto U = EXAMD_ARR(const float4, A.U, A.N, st);
@@ -360,6 +366,13 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     const uint4* src = reinterpret_cast<const uint4*>(&c_own);
     uint4* dst = reinterpret_cast<uint4*>(sown);
     for (int k = tid; k < (int)(sizeof(OwnLut) / 16); k += blockDim.x) dst[k] = src[k];
+    if (MULTI)
+      for (int k = tid; k < A.lj.nt * A.lj.nt; k += blockDim.x) {
+        if (FP64)
+          ljs64[k] = A.lj.p64[k];
+        else
+          ljs32[k] = A.lj.p32[k];
+      }
   }
   // Per-axis tables.  Ext coordinate l (cell X0 + l - 1, l = 0..E; l = E is
   // the far edge of the last ext cell) has origin (g0 + l - 1)*bl + n*r, with
@@ -528,10 +541,11 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     if (qn >= 32) {  // a batch only moves the ring's head
       __syncwarp();
       if (FP64)
-        force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
-                                            qh);
+        force_batch64<MULTI, ENERGY, COUNT>(32, qk, pd, code, img, B.L, fd, cap, A.lj, ljs64, esum, wsum, A.status,
+                                            nacc, qh);
       else
-        force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(32, qh, qd, fa, fr, cap, A, ek, wk, nacc, big_flag);
+        force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(32, qh, qd, fa, fr, cap, A, ljs32, ek, wk, nacc,
+                                                             big_flag);
       __syncwarp();
       qh = (qh + 32) & (kQueue - 1);
       qn -= 32;
@@ -544,7 +558,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     if (!acc) return;
     const int i = key & 0x3fff, m = (key >> 14) & 0x3fff;
     LJ32 P = A.lj.p32[0];
-    if (MULTI) P = A.lj.p32[((key >> 28) & 3) * A.lj.nt + ((unsigned)key >> 30)];
+    if (MULTI) P = ljs32[((key >> 28) & 3) * A.lj.nt + ((unsigned)key >> 30)];
     float dg = 0.f, e = 0.f;
     if (pair_fn32<false>(A.lj.pot, dq.w, P, dg, e) != 0) return;
     const float dgs = kFix * dg;
@@ -624,7 +638,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int tj = __float_as_int(pj.w);
       const int kb = __float_as_int(a.w);
       if (COUNT && valid) ++neval;
-      const float thr = MULTI ? A.lj.p32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
+      const float thr = MULTI ? ljs32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
       // disjoint bit fields: the sum is the OR, in one instruction
       const int key = (int)((unsigned)kb + ((unsigned)m << 14) + (MULTI ? (unsigned)tj << 30 : 0u));
       if (MODE == kRedoBig)
@@ -941,10 +955,11 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   if (qn > 0) {  // the last, partial batch
     __syncwarp();
     if (FP64)
-      force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, esum, wsum, A.status, nacc,
-                                          qh);
+      force_batch64<MULTI, ENERGY, COUNT>(qn, qk, pd, code, img, B.L, fd, cap, A.lj, ljs64, esum, wsum, A.status,
+                                          nacc, qh);
     else
-      force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(qn, qh, qd, fa, fr, cap, A, ek, wk, nacc, big_flag);
+      force_batch<MULTI, ENERGY, COUNT, MODE == kRedoFull>(qn, qh, qd, fa, fr, cap, A, ljs32, ek, wk, nacc,
+                                                           big_flag);
   }
   __syncthreads();
   // a large term was left out: list the tile for the redo pass
