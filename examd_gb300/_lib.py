@@ -53,6 +53,8 @@ class Params(C.Structure):
         ("potential", C.c_int),
         ("pair_tables", C.c_int),
         ("tile_balance", C.c_int),
+        ("pair_skin", C.c_double),
+        ("pair_list_capacity", C.c_int),
     ]
 
 
@@ -97,6 +99,7 @@ def load():
             "examd_gpu_run": (C.c_int, [ctxp, C.c_int, C.c_double, C.c_int, dp, C.POINTER(Stats)]),
             "examd_gpu_prepare_run": (C.c_int, [ctxp, C.c_double, C.c_int, C.c_int]),
             "examd_gpu_time_phases": (C.c_int, [ctxp, C.c_int, C.c_double, dp]),
+            "examd_gpu_list_info": (C.c_int, [ctxp, i64p, ip, ip, ip]),
             "examd_gpu_get_state": (C.c_int, [ctxp, dp, dp]),
             "examd_gpu_kinetic": (C.c_int, [ctxp, dp]),
             "examd_kinetic_static": (C.c_int, [C.c_int, C.c_int64, C.c_int, i64p, vp, vp, vp, vp, C.c_int, dp, dp,

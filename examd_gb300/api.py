@@ -48,7 +48,7 @@ PAIR_TABLES = {"auto": 0, "wide": 1, "compact": 2}
 
 def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None, block_length=None,
            tile=None, warps=None, strict_box=False, device=0, potential="lj", pair_tables="auto",
-           tile_balance=0):
+           tile_balance=0, pair_skin=0.0, pair_list_capacity=0):
     """examd_params and the examd_box array of a system, from Python arguments."""
     lib = _L.load()
     b = np.atleast_2d(np.asarray(boxes, dtype=np.float64))
@@ -85,6 +85,8 @@ def _setup(boxes, natoms, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, 
     if tile_balance not in (0, 1):
         raise ValueError("tile_balance must be 0 (split by cell count) or 1 (by width)")
     p.tile_balance = int(tile_balance)
+    p.pair_skin = float(pair_skin)
+    p.pair_list_capacity = int(pair_list_capacity)
     arr = (_L.Box * b.shape[0])()
     for k in range(b.shape[0]):
         for a in range(3):
@@ -124,13 +126,18 @@ class MidpointLJ:
     mixed form's per-warp tables, "auto" (compact where that fits more CTAs
     on an SM), "wide" or "compact"; the forces are the same bit for bit.
     tile_balance: 0 splits each axis into tiles by cell count, 1 by width (the
-    wide last cell that absorbs the box's remainder counts as two)."""
+    wide last cell that absorbs the box's remainder counts as two).
+    pair_skin: 0 (the reference's schedule: cells and candidate pairs at
+    every evaluation) or, mixed form, the skin of the per-tile pair lists
+    (rebuilt when an atom has moved more than half of it); pair_list_capacity:
+    list entries per atom (0: sized by the library)."""
 
     def __init__(self, boxes, natoms, *, precision=FP64, eps=1.0, sigma=1.0, rc=2.5, ntypes=1, mass=None,
                  block_length=None, tile=None, warps=None, strict_box=False, device=0, potential="lj",
-                 pair_tables="auto", tile_balance=0):
+                 pair_tables="auto", tile_balance=0, pair_skin=0.0, pair_list_capacity=0):
         lib, p, arr, b, n, m = _setup(boxes, natoms, precision, eps, sigma, rc, ntypes, mass, block_length, tile,
-                                      warps, strict_box, device, potential, pair_tables, tile_balance)
+                                      warps, strict_box, device, potential, pair_tables, tile_balance, pair_skin,
+                                      pair_list_capacity)
         self._lib = lib
         self.nboxes = int(b.shape[0])
         self.natoms = n.copy()
@@ -239,6 +246,15 @@ class MidpointLJ:
         ms = np.zeros(3)
         self._chk(self._lib.examd_gpu_time_phases(self._ctx, int(nsteps), float(dt), _d(ms)), "examd_gpu_time_phases")
         return {"kick_bin_count": float(ms[0]), "bin_scan_scatter": float(ms[1]), "pair": float(ms[2])}
+
+    def list_info(self):
+        """Pair-list mode: builds so far, list entries per atom, the most entries of one atom at the builds
+        since the last call and the tiles computed by enumeration (zeros without pair lists)."""
+        b = C.c_int64()
+        c, l, f = C.c_int(), C.c_int(), C.c_int()
+        self._chk(self._lib.examd_gpu_list_info(self._ctx, C.byref(b), C.byref(c), C.byref(l), C.byref(f)),
+                  "examd_gpu_list_info")
+        return {"builds": b.value, "capacity": c.value, "longest": l.value, "fallback_tiles": f.value}
 
     def state(self):
         pos = np.zeros((self.n, 3))

@@ -219,9 +219,26 @@ struct examd_ctx {
   bool forces_valid = false;  // Fown/P hold F(X[cur])
   bool energy_valid = false;
 
+  // pair-list mode (examd_params.pair_skin > 0): the offsets Ub of the last
+  // build, the per-tile lists (lslots staged atoms of lk entries each) and
+  // their counts, the staged atoms per tile, the fallback tiles and the list
+  // words (ListWord); list_gen counts the reallocations of the lists (a
+  // captured graph names one generation)
+  bool list = false;
+  float disp_thr2 = 0.f;  // rebuild when an atom moved more than this squared
+  float4* Ub = nullptr;
+  unsigned short* plist = nullptr;
+  unsigned short* plcnt = nullptr;
+  int lk = 0, lslots = 0, list_gen = 0;
+  int* lcount = nullptr;
+  int* fb = nullptr;
+  int* lw = nullptr;
+  int* h_lw = nullptr;  // pinned host copy of the list words
+  int64_t host_builds = 0;  // builds the host asked for (the device counts the others)
+
   // graph cache
   cudaGraphExec_t gexec = nullptr;
-  int g_parity = -1, g_chunk = 0, g_energy = -1, g_cap = 0;
+  int g_parity = -1, g_chunk = 0, g_energy = -1, g_cap = 0, g_list_gen = 0;
   double g_dt = 0.0;
   // the force call at new positions (examd_gpu_forces_at) as a CUDA graph,
   // one per parity of the sort's double buffer, for a caller that passes the
@@ -229,7 +246,7 @@ struct examd_ctx {
   struct IoGraph {
     cudaGraphExec_t exec = nullptr;
     const void *pos = nullptr, *forces = nullptr, *epot = nullptr, *virial = nullptr;
-    int accumulate = -1, cap = 0, cap_redo = 0;
+    int accumulate = -1, cap = 0, cap_redo = 0, list_gen = 0;
     bool pack = false;
   } io_graph[2];
 
@@ -268,7 +285,8 @@ void free_all(examd_ctx* ctx) {
                   ctx->cellOld, ctx->slot, ctx->count, ctx->cstart, ctx->bsum,
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
                   ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor,
-                  ctx->d_atom0, ctx->keAtom, ctx->partial, ctx->redo, ctx->redo_n};
+                  ctx->d_atom0, ctx->keAtom, ctx->partial, ctx->redo, ctx->redo_n,
+                  ctx->Ub, ctx->plist, ctx->plcnt, ctx->lcount, ctx->fb, ctx->lw};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (int b = 0; b < 2; ++b) {
@@ -280,6 +298,7 @@ void free_all(examd_ctx* ctx) {
     if (ctx->id[b]) cudaFree(ctx->id[b]);
   }
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
+  if (ctx->h_lw) cudaFreeHost(ctx->h_lw);
   if (ctx->inv) cudaFree(ctx->inv);
   for (cudaEvent_t e : ctx->ev_io)
     if (e) cudaEventDestroy(e);
@@ -402,8 +421,15 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
       if (p.eps[k] != p.eps[kt] || p.sigma[k] != p.sigma[kt] || p.rc[k] != p.rc[kt]) return EXAMD_ERR_ARG;
       rcmax = std::max(rcmax, p.rc[k]);
     }
-  double want = p.cell_edge > 0 ? p.cell_edge : 0.5 * rcmax;
-  if (want < 0.5 * rcmax) return EXAMD_ERR_ARG;
+  // pair-list mode: the cells must hold every pair within rc + skin in the
+  // 63-entry table's reach, so their edge is at least (rc + skin) / 2
+  const double skin = p.pair_skin;
+  if (!(skin >= 0.0) || !std::isfinite(skin) || (skin > 0.0 && p.precision != EXAMD_MIXED)) return EXAMD_ERR_ARG;
+  if (skin > 0.0 && skin < 1e-3) return EXAMD_ERR_ARG;  // below the displacement test's margin
+  if (p.pair_list_capacity < 0 || p.pair_list_capacity > 1024 || p.pair_list_capacity % 8 != 0) return EXAMD_ERR_ARG;
+  const double reach = rcmax + skin;
+  double want = p.cell_edge > 0 ? p.cell_edge : 0.5 * reach;
+  if (want < 0.5 * reach) return EXAMD_ERR_ARG;
   double bl;
   int blq = 0, blk = 0;
   if (round_block_length(want, &bl, &blq, &blk) != EXAMD_OK) return EXAMD_ERR_ARG;
@@ -433,6 +459,11 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     delete ctx;
     return EXAMD_ERR_ARG;
   }
+  ctx->list = skin > 0.0;
+  ctx->pc.list = ctx->list;
+  // an atom that moved d since the build is tested in FP32 against skin/2
+  // less a margin of 1e-4 that covers the offsets' rounding many times over
+  ctx->disp_thr2 = ctx->list ? (float)((0.5 * skin - 1e-4) * (0.5 * skin - 1e-4)) : 0.f;
   ctx->pc.warps = p.warps > 0 ? p.warps : 8;
   if (ctx->pc.warps < 4 || ctx->pc.warps > 8) {
     delete ctx;
@@ -480,6 +511,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     lj.p32[k].rc2 = (float)(r * r);
     lj.p32[k].rcut2 = (float)rcut2;
     lj.p32[k].eshift = (float)eshift;
+    lj.p32[k].rl2 = (float)((r + skin) * (r + skin));
     {
       // |F(r)| = 24 eps (2 s^12 - s^6) / r, s = sigma / r, falls monotonically
       // from r -> 0 to its zero at 2^(1/6) sigma: bisect for |F| = kFixMaxForce,
@@ -503,7 +535,11 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     rc2max = std::max(rc2max, lj.p32[k].rc2);
   }
   lj.rc2max = rc2max;
-  lj.prune2 = (float)((rcmax + 1e-4) * (rcmax + 1e-4));
+  // pair-list mode: atoms may be up to skin/2 outside the cells they were
+  // sorted into, so an enumeration between builds prunes at rc + skin/2
+  const double reach_now = rcmax + 0.5 * skin + 1e-4;
+  lj.prune2 = (float)(reach_now * reach_now);
+  lj.prune2_list = (float)((reach + 1e-4) * (reach + 1e-4));
   for (int a = 0; a < EXAMD_MAX_TYPES; ++a) {
     double m = (a < nt && p.mass[a] > 0) ? p.mass[a] : 1.0;
     lj.mass[a] = m;
@@ -740,6 +776,18 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   ALLOC(ctx->d_atom0, nboxes + 1);
   ALLOC(ctx->keAtom, N);
   ALLOC(ctx->inv, N);
+  if (ctx->list) {
+    ALLOC(ctx->Ub, N);
+    ALLOC(ctx->lcount, ctx->ntiles);
+    ALLOC(ctx->fb, ctx->ntiles);
+    ALLOC(ctx->lw, LW_WORDS);
+    if (cudaHostAlloc((void**)&ctx->h_lw, LW_WORDS * sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+      ctx->h_lw = nullptr;
+      free_all(ctx);
+      delete ctx;
+      return EXAMD_ERR_NOMEM;
+    }
+  }
   {
     int64_t maxa = 1, maxt = 1;
     for (int b = 0; b < nboxes; ++b) {
@@ -766,6 +814,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
             cudaMemsetAsync(ctx->count, 0, NC * sizeof(int), st) == cudaSuccess &&
             cudaMemsetAsync(ctx->status, 0, sizeof(int), st) == cudaSuccess &&
             (!ctx->redo_n || cudaMemsetAsync(ctx->redo_n, 0, 2 * sizeof(int), st) == cudaSuccess) &&
+            (!ctx->lw || cudaMemsetAsync(ctx->lw, 0, LW_WORDS * sizeof(int), st) == cudaSuccess) &&
             cudaStreamSynchronize(st) == cudaSuccess;
   if (!ok) {
     free_all(ctx);
@@ -793,23 +842,36 @@ inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t
 
 // Scan and final ordering after a counting pass; swaps the buffers.
 // want_inv: also record the caller -> sorted map (for the caller-order I/O).
-int finish_binning(examd_ctx* ctx, bool want_inv) {
+// Pair-list mode: the sorted arrays are copied back into the current buffer
+// (a step loop captured as a graph names fixed buffers, and whether a step
+// rebuilds is decided on the device), the offsets are kept as the build's
+// Ub, the caller map is always recorded, and gate (a device word, or
+// nullptr) makes the whole sequence conditional.
+int finish_binning(examd_ctx* ctx, bool want_inv, const int* gate = nullptr) {
   cudaStream_t st = ctx->st;
   const int nc = ctx->NC;
   const int nsb = (nc + kScanTileHost - 1) / kScanTileHost;
   const int s = ctx->cur, d = 1 - ctx->cur;
-  k_scan_reduce<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum);
-  k_scan_final<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum, ctx->cstart);
+  const bool list = ctx->list;
+  if (list) want_inv = true;
+  k_scan_reduce<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum, gate);
+  k_scan_final<<<nsb, 256, 0, st>>>(nc, ctx->count, ctx->bsum, ctx->cstart, gate);
   if (ctx->N > 0) {
     k_finalize<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, ctx->cellOld, ctx->slot, ctx->cstart, ctx->d_boxes,
                                               ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->V[s][0],
                                               ctx->V[s][1], ctx->V[s][2], ctx->meta[s], ctx->id[s],
                                               ctx->X[d][0], ctx->X[d][1], ctx->X[d][2], ctx->V[d][0],
                                               ctx->V[d][1], ctx->V[d][2], ctx->meta[d], ctx->id[d], ctx->U,
-                                              ctx->cellS, want_inv ? ctx->inv : nullptr, ctx->NC, ctx->status);
+                                              list ? ctx->Ub : nullptr, ctx->cellS, want_inv ? ctx->inv : nullptr,
+                                              ctx->NC, ctx->status, gate);
+    if (list)
+      k_copy_back<<<nblk(ctx->N), 256, 0, st>>>(ctx->N, ctx->X[d][0], ctx->X[d][1], ctx->X[d][2], ctx->V[d][0],
+                                                 ctx->V[d][1], ctx->V[d][2], ctx->meta[d], ctx->id[d], ctx->X[s][0],
+                                                 ctx->X[s][1], ctx->X[s][2], ctx->V[s][0], ctx->V[s][1],
+                                                 ctx->V[s][2], ctx->meta[s], ctx->id[s], gate);
   }
   CK(cudaGetLastError());
-  ctx->cur = d;
+  if (!list) ctx->cur = d;
   ctx->inv_valid = want_inv;
   return EXAMD_OK;
 }
@@ -855,7 +917,8 @@ int check_status(examd_ctx* ctx) {
 // headroom for the FP64 form and for the mixed form's redo pass; +6% + 32 for
 // the mixed form's first pass (a tile that outgrows it before the next update
 // is computed in full by the redo pass, at the redo capacity).
-int update_capacity(examd_ctx* ctx) {
+int update_capacity(examd_ctx* ctx, bool* grew = nullptr) {
+  if (grew) *grew = false;
   CK(cudaMemsetAsync(ctx->d_occ, 0, 2 * sizeof(int), ctx->st));
   k_tile_occupancy<<<ctx->ntiles, 128, 0, ctx->st>>>(ctx->d_tiles, ctx->d_boxes, ctx->cstart, ctx->d_occ);
   CK(cudaGetLastError());
@@ -894,6 +957,7 @@ int update_capacity(examd_ctx* ctx) {
   ctx->cap = want;
   ctx->cap_redo = want_r;
   ctx->smem = bytes;
+  if (grew) *grew = true;
   // all variants used by this context
   PairConfig c = ctx->pc;
   for (int e = 0; e < 2; ++e)
@@ -930,10 +994,163 @@ PairArgs pair_args(examd_ctx* ctx) {
   a.redo = ctx->redo;
   a.redo_n = ctx->redo_n;
   a.redo_done = (unsigned*)(ctx->redo_n + 1);
+  a.list = ctx->plist;
+  a.lcnt = ctx->plcnt;
+  a.lcount = ctx->lcount;
+  a.lk = ctx->lk;
+  a.lslots = ctx->lslots;
+  a.ntiles = ctx->ntiles;
+  a.fb = ctx->fb;
+  a.lw = ctx->lw;
+  a.gate = nullptr;
   return a;
 }
 
-int run_pair(examd_ctx* ctx, bool energy, bool count, double* boxE = nullptr, double* boxW = nullptr) {
+// Pair-list mode: the lists of every tile at the current cells.  gate: a
+// device word that makes the build conditional (the step loop), or nullptr:
+// build now, with the fallback list emptied first.
+int build_lists(examd_ctx* ctx, const int* gate) {
+  if (!gate) {
+    CK(cudaMemsetAsync(ctx->lw + LW_FBN, 0, sizeof(int), ctx->st));
+    ++ctx->host_builds;
+  }
+  PairArgs a = pair_args(ctx);
+  a.gate = gate;
+  CK(launch_pair_build(ctx->pc, a, ctx->ntiles, ctx->smem, ctx->st));
+  return EXAMD_OK;
+}
+
+// Pair-list mode: cells and lists rebuilt at the current positions (gate as
+// for build_lists).
+int rebuild(examd_ctx* ctx, const int* gate) {
+  const int s = ctx->cur;
+  if (ctx->N > 0) {
+    k_bin_count<<<nblk(ctx->N), 256, 0, ctx->st>>>(ctx->N, ctx->X[s][0], ctx->X[s][1], ctx->X[s][2],
+                                                    ctx->meta[s], ctx->d_boxes, ctx->cellOld, ctx->slot,
+                                                    ctx->count, ctx->status, gate);
+    CK(cudaGetLastError());
+  }
+  const int rc = finish_binning(ctx, true, gate);
+  return rc ? rc : build_lists(ctx, gate);
+}
+
+// Pair-list mode, after new positions: the device decides whether some atom
+// moved more than half the skin since the build (or a rebuild was asked
+// for), and the rebuild's kernels run or return at once on that decision.
+int maybe_rebuild(examd_ctx* ctx) {
+  k_list_decide<<<1, 1, 0, ctx->st>>>(ctx->lw, ctx->disp_thr2);
+  CK(cudaGetLastError());
+  return rebuild(ctx, ctx->lw + LW_GATE);
+}
+
+// Pair-list mode: lists of `want` entries per staged atom, for the current
+// staged-atom capacity.  The captured graphs name the old lists, so they are
+// dropped.
+int set_list_capacity(examd_ctx* ctx, int want) {
+  const int slots = (ctx->cap + 31) & ~31;
+  if (want == ctx->lk && slots == ctx->lslots && ctx->plist) return EXAMD_OK;
+  CK(cudaStreamSynchronize(ctx->st));
+  if (ctx->plist) cudaFree(ctx->plist);
+  if (ctx->plcnt) cudaFree(ctx->plcnt);
+  ctx->plist = nullptr;
+  ctx->plcnt = nullptr;
+  ctx->lk = ctx->lslots = 0;
+  const size_t atoms = (size_t)ctx->ntiles * (size_t)slots;
+  int rc = dalloc(ctx, &ctx->plist, atoms * (size_t)want);
+  if (rc) return rc;
+  rc = dalloc(ctx, &ctx->plcnt, atoms);
+  if (rc) return rc;
+  ctx->lk = want;
+  ctx->lslots = slots;
+  ++ctx->list_gen;
+  if (ctx->gexec) {
+    cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+  }
+  for (auto& g : ctx->io_graph) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = examd_ctx::IoGraph{};
+  }
+  return EXAMD_OK;
+}
+
+// Pair-list mode: the list words, read after the stream's work; the longest
+// list since the last read is reset.
+int read_list_words(examd_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->h_lw, ctx->lw, LW_WORDS * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemsetAsync(ctx->lw + LW_LMAX, 0, sizeof(int), ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return EXAMD_OK;
+}
+
+// entries per atom: a multiple of 8 (a list pass reads eight at a time), at
+// most 1024 (the list pass's count histogram)
+int list_capacity_for(int longest) { return std::min(((longest + longest / 5 + 8) + 7) & ~7, 1024); }
+
+// Pair-list mode, after a binning with the atoms in their cells: the lists
+// built now at a capacity that fits the atom with the most entries, with 20 %
+// headroom (the first build at an estimate from the densest box: 1.6 times
+// the pairs in half a sphere of radius rc + skin).
+int init_lists(examd_ctx* ctx) {
+  if (ctx->p.pair_list_capacity > 0) {  // the caller's capacity, never resized
+    const int rc = set_list_capacity(ctx, ctx->p.pair_list_capacity);
+    return rc ? rc : build_lists(ctx, nullptr);
+  }
+  if (!ctx->plist) {
+    double rho = 0.0, reach = 0.0;
+    for (int b = 0; b < ctx->nboxes; ++b)
+      rho = std::max(rho, (double)ctx->boxes[b].natoms / (ctx->boxes[b].L[0] * ctx->boxes[b].L[1] * ctx->boxes[b].L[2]));
+    for (int k = 0; k < ctx->lj.nt * ctx->lj.nt; ++k) reach = std::max(reach, std::sqrt((double)ctx->lj.p32[k].rl2));
+    const double est = 1.6 * (2.0943951 * reach * reach * reach * rho) + 16.0;
+    const int rc = set_list_capacity(ctx, list_capacity_for((int)std::min(est, 4096.0)));
+    if (rc) return rc;
+  } else {
+    const int rc = set_list_capacity(ctx, ctx->lk);  // new slots if the staged-atom capacity grew
+    if (rc) return rc;
+  }
+  for (int it = 0; it < 4; ++it) {
+    int rc = build_lists(ctx, nullptr);
+    if (rc) return rc;
+    rc = read_list_words(ctx);
+    if (rc) return rc;
+    const int longest = ctx->h_lw[LW_LMAX];
+    const int want = list_capacity_for(longest);
+    if (longest <= ctx->lk && ctx->lk <= 2 * want) return EXAMD_OK;
+    rc = set_list_capacity(ctx, want);  // grow to fit, or shrink an estimate far too large
+    if (rc) return rc;
+  }
+  return EXAMD_OK;  // any tile still over its list is computed by enumeration
+}
+
+int run_pair(examd_ctx* ctx, bool energy, bool count, double* boxE = nullptr, double* boxW = nullptr);
+
+// Pair-list mode, between runs of steps: a tile with an atom whose list
+// outgrew its capacity since the last check, or with more staged atoms than
+// the lists have slots, is computed by enumeration meanwhile.  The lists get
+// room for it: new lists, which a build at the current positions fills, after
+// a fresh sort (a build needs every atom inside its cell), and the forces
+// again in the new order.  A staged-atom capacity that grew within the slots
+// makes the next step rebuild, so that the tiles over the old one get lists.
+int update_lists(examd_ctx* ctx, bool cap_grew) {
+  int rc = read_list_words(ctx);
+  if (rc) return rc;
+  const int longest = ctx->h_lw[LW_LMAX];
+  const bool fixed = ctx->p.pair_list_capacity > 0;
+  const int want = fixed ? ctx->lk : std::max(ctx->lk, list_capacity_for(longest));
+  if (want != ctx->lk || ctx->cap > ctx->lslots) {
+    if ((rc = set_list_capacity(ctx, want)) || (rc = rebuild(ctx, nullptr)) || (rc = run_pair(ctx, false, false)))
+      return rc;
+    return read_list_words(ctx);
+  }
+  if (cap_grew) {
+    const int one = 1;
+    CK(cudaMemcpyAsync(ctx->lw + LW_FORCE, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  return EXAMD_OK;
+}
+
+int run_pair(examd_ctx* ctx, bool energy, bool count, double* boxE, double* boxW) {
   PairConfig c = ctx->pc;
   c.energy = energy;
   c.count = count;
@@ -1065,6 +1282,13 @@ int examd_gpu_set_atoms(examd_ctx* ctx, int64_t n, const double* pos, const int*
   if (rc) return rc;
   rc = update_capacity(ctx);
   if (rc) return rc;
+  if (ctx->list) {
+    CK(cudaMemsetAsync(ctx->lw, 0, LW_WORDS * sizeof(int), st));
+    rc = init_lists(ctx);
+    if (rc) return rc;
+    rc = check_status(ctx);
+    if (rc) return rc;
+  }
   ctx->atoms_set = true;
   ctx->forces_valid = false;
   return EXAMD_OK;
@@ -1101,14 +1325,20 @@ int enqueue_forces_at(examd_ctx* ctx, const double* pos, double* forces, double*
                          cudaMemcpyHostToDevice, st2));
       CK(cudaEventRecord(ctx->ev_io[c], st2));
       CK(cudaStreamWaitEvent(st, ctx->ev_io[c], 0));
-      k_gather_pos_bin_range<<<nblk(i1 - i0), 256, 0, st>>>(i0, i1, ctx->stage2, ctx->d_boxes, ctx->p.strict_box,
-                                                            ctx->X[s][0], ctx->X[s][1], ctx->X[s][2], ctx->meta[s],
-                                                            ctx->inv, ctx->cellOld, ctx->slot, ctx->count,
-                                                            ctx->status);
-      CK(cudaGetLastError());
+      if (ctx->list) {
+        CK(launch_gather_pos_list(i0, i1, ctx->stage2, ctx->d_boxes, ctx->p.strict_box, ctx->X[s][0],
+                                  ctx->X[s][1], ctx->X[s][2], ctx->meta[s], ctx->inv, ctx->cellS, ctx->U, ctx->Ub,
+                                  ctx->lw, ctx->status, st));
+      } else {
+        k_gather_pos_bin_range<<<nblk(i1 - i0), 256, 0, st>>>(i0, i1, ctx->stage2, ctx->d_boxes,
+                                                              ctx->p.strict_box, ctx->X[s][0], ctx->X[s][1],
+                                                              ctx->X[s][2], ctx->meta[s], ctx->inv, ctx->cellOld,
+                                                              ctx->slot, ctx->count, ctx->status);
+        CK(cudaGetLastError());
+      }
     }
   }
-  int rc = finish_binning(ctx, true);
+  int rc = ctx->list ? maybe_rebuild(ctx) : finish_binning(ctx, true);
   if (rc) return rc;
   return enqueue_forces(ctx, forces, epot, virial, accumulate);
 }
@@ -1135,7 +1365,7 @@ int examd_gpu_forces_at(examd_ctx* ctx, const double* pos, double* forces, doubl
   auto& g = ctx->io_graph[ctx->cur];
   const bool hit = g.exec && g.pos == pos && g.forces == forces && g.epot == epot && g.virial == virial &&
                    g.accumulate == accumulate && g.cap == ctx->cap && g.cap_redo == ctx->cap_redo &&
-                   g.pack == ctx->pc.pack;
+                   g.pack == ctx->pc.pack && g.list_gen == ctx->list_gen;
   if (!hit) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = examd_ctx::IoGraph{};
@@ -1161,9 +1391,10 @@ int examd_gpu_forces_at(examd_ctx* ctx, const double* pos, double* forces, doubl
     g.cap = ctx->cap;
     g.cap_redo = ctx->cap_redo;
     g.pack = ctx->pc.pack;
+    g.list_gen = ctx->list_gen;
   }
   CK(cudaGraphLaunch(g.exec, ctx->st));
-  ctx->cur = 1 - ctx->cur;  // the host-side effects of the captured call
+  if (!ctx->list) ctx->cur = 1 - ctx->cur;  // the host-side effects of the captured call
   ctx->inv_valid = true;
   return finish_forces(ctx);
 }
@@ -1200,15 +1431,21 @@ KickArgs kick_args(examd_ctx* ctx, double ckick, double dt, bool drift, double h
   k.slot = ctx->slot;
   k.count = ctx->count;
   k.status = ctx->status;
+  k.list = ctx->list;
+  k.U = ctx->U;
+  k.Ub = ctx->Ub;
+  k.lw = ctx->lw;
   return k;
 }
 
 // One step after the first: kick(ck) + drift + bin, pair.  keSlot receives the
 // kinetic energy at the start of this step, eSlot the potential energy after.
+// Pair-list mode: the binning and the lists only on the steps that the
+// device decides to rebuild.
 int step_once(examd_ctx* ctx, double ck, double dt, double* keSlot, double* eSlot, double* wSlot) {
   const double h = 0.5 * dt;
   CK(launch_kick(kick_args(ctx, ck, dt, true, keSlot ? h : 0.0, keSlot), ctx->st));
-  int rc = finish_binning(ctx, false);
+  int rc = ctx->list ? maybe_rebuild(ctx) : finish_binning(ctx, false);
   if (rc) return rc;
   return run_pair(ctx, eSlot != nullptr, false, eSlot, wSlot);
 }
@@ -1242,9 +1479,10 @@ int ensure_ebuf(examd_ctx* ctx, int steps) {
 // graph for buffer parity `parity`, captured and instantiated unless the
 // cached one already matches.  Captures only: no step runs.
 int ensure_chunk_graph(examd_ctx* ctx, int chunk, double dt, bool wantE, int parity) {
-  const bool rebuild = !ctx->gexec || ctx->g_parity != parity || ctx->g_chunk != chunk ||
-                       ctx->g_energy != (int)wantE || ctx->g_dt != dt || ctx->g_cap != ctx->cap;
-  if (!rebuild) return EXAMD_OK;
+  const bool stale = !ctx->gexec || ctx->g_parity != parity || ctx->g_chunk != chunk ||
+                     ctx->g_energy != (int)wantE || ctx->g_dt != dt || ctx->g_cap != ctx->cap ||
+                     ctx->g_list_gen != ctx->list_gen;
+  if (!stale) return EXAMD_OK;
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   ctx->gexec = nullptr;
   const int nb = ctx->nboxes;
@@ -1257,7 +1495,8 @@ int ensure_chunk_graph(examd_ctx* ctx, int chunk, double dt, bool wantE, int par
     src = step_once(ctx, dt, dt, wantE ? ctx->boxKE + (size_t)j * nb : nullptr,
                     wantE ? ctx->boxE + (size_t)j * nb : nullptr, wantE ? ctx->boxW + (size_t)j * nb : nullptr);
   cudaError_t ce = cudaStreamEndCapture(ctx->st, &g);
-  // capture advanced the host-side parity; the graph leaves it unchanged (chunk even)
+  // capture advanced the host-side parity; the graph leaves it unchanged (chunk
+  // even; pair-list mode: no step swaps the buffers)
   ctx->cur = saved;
   if (src != EXAMD_OK) return src;
   if (ce != cudaSuccess) return ctx->cuda_fail(ce, "cudaStreamEndCapture");
@@ -1272,6 +1511,7 @@ int ensure_chunk_graph(examd_ctx* ctx, int chunk, double dt, bool wantE, int par
   ctx->g_energy = wantE;
   ctx->g_dt = dt;
   ctx->g_cap = ctx->cap;
+  ctx->g_list_gen = ctx->list_gen;
   return EXAMD_OK;
 }
 
@@ -1326,12 +1566,14 @@ int examd_gpu_run(examd_ctx* ctx, int nsteps, double dt, int graph_chunk, double
         CK(cudaStreamSynchronize(st));  // buffers are reused by the next replay
       }
       done += chunk;
-      // the capacity may need to grow as the density fluctuates
+      // the capacities may need to grow as the density fluctuates
       CK(cudaStreamSynchronize(st));
       rc = check_status(ctx);
       if (rc) return rc;
-      rc = update_capacity(ctx);
+      bool grew = false;
+      rc = update_capacity(ctx, &grew);
       if (rc) return rc;
+      if (ctx->list && (rc = update_lists(ctx, grew))) return rc;
     } else {
       double* ke = nullptr;
       if (wantE) ke = ctx->boxKE;
@@ -1391,8 +1633,8 @@ int examd_gpu_prepare_run(examd_ctx* ctx, double dt, int graph_chunk, int energi
   }
   if (chunk == 0) return EXAMD_OK;
   // the run's first step flips the sort's double buffer: its graph chunks
-  // run at the other parity
-  rc = ensure_chunk_graph(ctx, chunk, dt, energies != 0, 1 - ctx->cur);
+  // run at the other parity (pair-list mode: at this one)
+  rc = ensure_chunk_graph(ctx, chunk, dt, energies != 0, ctx->list ? ctx->cur : 1 - ctx->cur);
   if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->st));
   return EXAMD_OK;
@@ -1415,7 +1657,7 @@ int examd_gpu_time_phases(examd_ctx* ctx, int nsteps, double dt, double* ms) {
     CK(cudaEventRecord(ctx->e0, st));
     CK(launch_kick(kick_args(ctx, dt, dt, true, 0.0, nullptr), st));
     CK(cudaEventRecord(ctx->e1, st));
-    rc = finish_binning(ctx, false);
+    rc = ctx->list ? maybe_rebuild(ctx) : finish_binning(ctx, false);
     if (rc) return rc;
     CK(cudaEventRecord(ctx->e2, st));
     rc = run_pair(ctx, false, false);
@@ -1433,6 +1675,26 @@ int examd_gpu_time_phases(examd_ctx* ctx, int nsteps, double dt, double* ms) {
   rc = check_status(ctx);
   if (rc) return rc;
   for (int a = 0; a < 3; ++a) ms[a] = acc[a] / nsteps;
+  return EXAMD_OK;
+}
+
+int examd_gpu_list_info(examd_ctx* ctx, int64_t* builds, int* capacity, int* longest, int* fallback_tiles) {
+  if (!ctx) return EXAMD_ERR_ARG;
+  int64_t b = 0;
+  int c = 0, l = 0, f = 0;
+  if (ctx->list) {
+    cudaSetDevice(ctx->dev);
+    const int rc = read_list_words(ctx);
+    if (rc) return rc;
+    b = ctx->h_lw[LW_BUILDS] + ctx->host_builds;
+    c = ctx->lk;
+    l = ctx->h_lw[LW_LMAX];
+    f = ctx->h_lw[LW_FBN];
+  }
+  if (builds) *builds = b;
+  if (capacity) *capacity = c;
+  if (longest) *longest = l;
+  if (fallback_tiles) *fallback_tiles = f;
   return EXAMD_OK;
 }
 
@@ -1506,7 +1768,11 @@ int examd_gpu_counters(examd_ctx* ctx, int64_t* candidates, int64_t* accepted, i
   if (!ctx) return EXAMD_ERR_ARG;
   if (!ctx->atoms_set) return EXAMD_ERR_STATE;
   cudaSetDevice(ctx->dev);
-  int rc = run_pair(ctx, false, true);
+  int rc;
+  // pair-list mode: the counts are the enumeration's, which needs every atom
+  // inside its cell: a fresh sort and lists first
+  if (ctx->list && (rc = rebuild(ctx, nullptr))) return rc;
+  rc = run_pair(ctx, false, true);
   if (rc) return rc;
   std::vector<long long> c(3 * (size_t)ctx->ntiles);
   CK(cudaMemcpyAsync(c.data(), ctx->tileC, c.size() * sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));

@@ -120,8 +120,9 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* sh, int& total) 
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(int nc, const int* __restrict__ count,
-                                                              int* __restrict__ bsum) {
+                                                              int* __restrict__ bsum, const int* gate) {
   __shared__ int sh[kScanThreads / 32];
+  if (gate && !*gate) return;
   int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   int s = 0;
 #pragma unroll
@@ -137,8 +138,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(int nc, const int*
 // over a separate scan of them.
 __global__ void __launch_bounds__(kScanThreads) k_scan_final(int nc, int* __restrict__ count,
                                                              const int* __restrict__ bsum,
-                                                             int* __restrict__ cstart) {
+                                                             int* __restrict__ cstart, const int* gate) {
   __shared__ int sh[kScanThreads / 32];
+  if (gate && !*gate) return;
   int pre = 0;
   for (int k = threadIdx.x; k < (int)blockIdx.x; k += blockDim.x) pre += bsum[k];
   int offset;
@@ -167,7 +169,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(int nc, int* __rest
 // counting pass, and each per-atom array is scattered into the other buffer.
 // The pair kernel's FP32 cell offsets U are computed here from the FP64
 // position (the same exact rule as the cell), not carried from the counting
-// pass: 32 B less memory traffic per atom.
+// pass: 32 B less memory traffic per atom.  Pair-list mode: the offsets are
+// also kept as Ub, the reference for the displacement test of later steps.
 __global__ void k_finalize(int64_t n, const int* __restrict__ cellOld, const int* __restrict__ slot,
                            const int* __restrict__ cstart, const BoxDev* __restrict__ boxes,
                            const double* __restrict__ X0, const double* __restrict__ X1,
@@ -176,8 +179,10 @@ __global__ void k_finalize(int64_t n, const int* __restrict__ cellOld, const int
                            const int* __restrict__ meta, const int* __restrict__ id, double* __restrict__ Y0,
                            double* __restrict__ Y1, double* __restrict__ Y2, double* __restrict__ W0,
                            double* __restrict__ W1, double* __restrict__ W2, int* __restrict__ meta2,
-                           int* __restrict__ id2, float4* __restrict__ U, int* __restrict__ cellS,
-                           int* __restrict__ inv, int nc, int* __restrict__ status) {
+                           int* __restrict__ id2, float4* __restrict__ U, float4* __restrict__ Ub,
+                           int* __restrict__ cellS, int* __restrict__ inv, int nc, int* __restrict__ status,
+                           const int* gate) {
+  if (gate && !*gate) return;
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int c = (int)EXAMD_IDX(cellOld[s], nc, status);
@@ -200,8 +205,57 @@ __global__ void k_finalize(int64_t n, const int* __restrict__ cellOld, const int
   cell_offset(z, B, 2, u.z);
   u.w = __int_as_float(mt & 0xff);
   U[d] = u;
+  if (Ub) Ub[d] = u;
   cellS[d] = c;
   if (inv) inv[EXAMD_IDX(myid, n, status)] = d;  // caller index -> sorted slot, when the caller's order is needed next
+}
+
+// Pair-list mode's binning count: the cell and slot of every atom at its
+// current position (the counting pass that the plain step fuses into the
+// kick, here only on the steps that rebuild).
+__global__ void k_bin_count(int64_t n, const double* __restrict__ X0, const double* __restrict__ X1,
+                            const double* __restrict__ X2, const int* __restrict__ meta,
+                            const BoxDev* __restrict__ boxes, int* __restrict__ cellOld, int* __restrict__ slot,
+                            int* __restrict__ count, int* __restrict__ status, const int* gate) {
+  if (gate && !*gate) return;
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  bin_one((int)s, X0[s], X1[s], X2[s], meta[s], boxes, cellOld, slot, count, status);
+}
+
+// Pair-list mode: the sorted arrays back into the primary buffer.
+__global__ void k_copy_back(int64_t n, const double* __restrict__ Y0, const double* __restrict__ Y1,
+                            const double* __restrict__ Y2, const double* __restrict__ W0,
+                            const double* __restrict__ W1, const double* __restrict__ W2,
+                            const int* __restrict__ meta2, const int* __restrict__ id2, double* __restrict__ X0,
+                            double* __restrict__ X1, double* __restrict__ X2, double* __restrict__ V0,
+                            double* __restrict__ V1, double* __restrict__ V2, int* __restrict__ meta,
+                            int* __restrict__ id, const int* gate) {
+  if (gate && !*gate) return;
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  X0[s] = Y0[s];
+  X1[s] = Y1[s];
+  X2[s] = Y2[s];
+  V0[s] = W0[s];
+  V1[s] = W1[s];
+  V2[s] = W2[s];
+  meta[s] = meta2[s];
+  id[s] = id2[s];
+}
+
+// Pair-list mode: one thread decides whether this step rebuilds and resets
+// the displacement maximum and the forced-rebuild request for the next step.
+// A rebuild empties the fallback list (the build fills it again).
+__global__ void k_list_decide(int* lw, float thr2) {
+  const int rb = (__int_as_float(lw[LW_DISP]) > thr2 || lw[LW_FORCE] != 0) ? 1 : 0;
+  lw[LW_GATE] = rb;
+  lw[LW_DISP] = 0;
+  lw[LW_FORCE] = 0;
+  if (rb) {
+    lw[LW_FBN] = 0;
+    lw[LW_BUILDS] += 1;
+  }
 }
 
 // inv[id[s]] = s: the caller-order map of the current sorted order.

@@ -36,6 +36,19 @@ enum StatusBits : int {
   ST_BOUNDS = 32,    // checked build: an index check failed (the access went to index 0)
 };
 
+// Pair-list mode: the device words that carry the list's state between the
+// kernels of a step (no host round trip, so that a step loop stays one CUDA
+// graph).
+enum ListWord : int {
+  LW_DISP = 0,    // largest squared displacement since the last build (float bits, atomicMax)
+  LW_GATE = 1,    // nonzero: this step rebuilds the cells and the lists (k_list_decide)
+  LW_FORCE = 2,   // nonzero: rebuild at the next step whatever the displacement
+  LW_FBN = 3,     // tiles in the fallback list (computed by enumeration every step)
+  LW_LMAX = 4,    // largest list length of a tile since the host last read it
+  LW_BUILDS = 5,  // builds since the context was created
+  LW_WORDS = 8
+};
+
 // Index-checked arrays of the checked build (-DEXAMD_CHECKED, the
 // counterpart of a memory checker on a pool where none may run): every
 // subscript is tested against the array's length; an index outside it sets
@@ -90,6 +103,7 @@ struct LJ32 {
   float sig2, m24eps, c4eps, rc2;  // m24eps = -24 eps (dg prefactor)
   float rcut2, eshift;
   float r2big;  // r^2 below which |F| >= kFixMaxForce (mixed form: left to the redo pass)
+  float rl2;    // pair-list mode: (rc + skin)^2, the list's cutoff for this type pair
 };
 
 // Mixed form: pair-force magnitude at which a term leaves the fixed-point sums
@@ -107,6 +121,9 @@ struct LJTable {
   int pot;       // EXAMD_POT_*
   float rc2max;
   float prune2;  // (max rc + 1e-4)^2: cell boxes farther than this hold no pair
+                 // (pair-list mode: (max rc + skin/2 + 1e-4)^2, atoms may have
+                 // left their cells by up to skin/2 since the list was built)
+  float prune2_list;  // pair-list mode: (max rc + skin + 1e-4)^2, for the list build
   LJ32 p32[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];
   LJ64 p64[EXAMD_MAX_TYPES * EXAMD_MAX_TYPES];
   double minv[EXAMD_MAX_TYPES];

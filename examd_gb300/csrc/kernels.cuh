@@ -14,13 +14,27 @@ __global__ void k_gather_pos_bin_range(int64_t i0, int64_t i1, const double* aos
                                        double* X0, double* X1, double* X2, const int* meta, const int* inv,
                                        int* cellOld, int* slot, int* count, int* status);
 __global__ void k_inverse(int64_t n, const int* id, int* inv);
-__global__ void k_scan_reduce(int nc, const int* count, int* bsum);
-__global__ void k_scan_final(int nc, int* count, const int* bsum, int* cstart);
+// gate: nullptr, or a device word; zero makes the launch return at once (the
+// pair-list mode's conditional rebuild inside a captured step loop).
+__global__ void k_scan_reduce(int nc, const int* count, int* bsum, const int* gate);
+__global__ void k_scan_final(int nc, int* count, const int* bsum, int* cstart, const int* gate);
 __global__ void k_finalize(int64_t n, const int* cellOld, const int* slot, const int* cstart, const BoxDev* boxes,
                            const double* X0, const double* X1, const double* X2, const double* V0,
                            const double* V1, const double* V2, const int* meta, const int* id, double* Y0,
                            double* Y1, double* Y2, double* W0, double* W1, double* W2, int* meta2, int* id2,
-                           float4* U, int* cellS, int* inv, int nc, int* status);
+                           float4* U, float4* Ub, int* cellS, int* inv, int nc, int* status, const int* gate);
+// Pair-list mode's rebuild: the binning count at the current positions, and
+// the sorted arrays copied back into the primary buffer (the step loop's
+// buffers stay fixed whether a step rebuilds or not).
+__global__ void k_bin_count(int64_t n, const double* X0, const double* X1, const double* X2, const int* meta,
+                            const BoxDev* boxes, int* cellOld, int* slot, int* count, int* status, const int* gate);
+__global__ void k_copy_back(int64_t n, const double* Y0, const double* Y1, const double* Y2, const double* W0,
+                            const double* W1, const double* W2, const int* meta2, const int* id2, double* X0,
+                            double* X1, double* X2, double* V0, double* V1, double* V2, int* meta, int* id,
+                            const int* gate);
+// Pair-list mode: decide whether this step rebuilds (largest displacement
+// since the build against thr2 = (skin/2 - margin)^2, or a forced rebuild).
+__global__ void k_list_decide(int* lw, float thr2);
 constexpr int kScanTileHost = 2048;  // cells per scan block (kScanThreads * kScanItems)
 
 // ---- pair.cu ----------------------------------------------------------------
@@ -50,6 +64,22 @@ struct PairArgs {
   int* redo;
   int* redo_n;
   unsigned* redo_done;
+  // pair-list mode: per tile and staged atom i (lslots slots, a multiple of
+  // 32), up to lk entries (a multiple of 8, at most 1024), the staged
+  // indices m of the pairs (i, m) that the tile owns within the list cutoff
+  // (list[tile][i][k]); their counts lcnt[tile][i]; per tile the staged
+  // atoms, or -1 when the tile is in the fallback list fb (computed by
+  // enumeration every step); the list words (ListWord); the build's gate
+  // (nullptr: build unconditionally)
+  unsigned short* list;
+  unsigned short* lcnt;
+  int* lcount;
+  int lk;
+  int lslots;
+  int ntiles;
+  int* fb;
+  int* lw;
+  const int* gate;
 };
 
 struct PairConfig {
@@ -58,6 +88,7 @@ struct PairConfig {
   bool pack = false;    // mixed form: compact per-warp tables (more CTAs per SM)
   bool energy = false;  // potential energy and virial
   bool count = false;   // candidate / accepted counters
+  bool list = false;    // mixed form: pair-list mode (forces from the per-tile lists)
   int warps = 8;
 };
 
@@ -68,6 +99,8 @@ cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes);  // opt-in smem
 // Resident CTAs per SM of the pair kernel at this capacity (occupancy calculator).
 int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max, int ext_max);
 cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st);
+// Pair-list mode: build the per-tile lists (gated by a.gate).
+cudaError_t launch_pair_build(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st);
 cudaError_t upload_own_lut(const OwnLut& lut);
 
 // ---- step.cu ----------------------------------------------------------------
@@ -118,8 +151,22 @@ struct KickArgs {
   int* slot;
   int* count;
   int* status;
+  // pair-list mode (drift only, instead of the binning count): the FP32
+  // offsets U from each atom's cell at the last build, and the largest
+  // squared displacement from the offsets Ub of that build (lw[LW_DISP])
+  bool list;
+  float4* U;
+  const float4* Ub;
+  int* lw;
 };
 cudaError_t launch_kick(const KickArgs& k, cudaStream_t st);
+// Pair-list mode: new positions for the caller's atoms [i0, i1) at their
+// sorted slots, with the offsets from their cells at the last build and the
+// displacement since then (the force call at new positions).
+cudaError_t launch_gather_pos_list(int64_t i0, int64_t i1, const double* aos, const BoxDev* boxes, int strict,
+                                   double* X0, double* X1, double* X2, const int* meta, const int* inv,
+                                   const int* cellS, float4* U, const float4* Ub, int* lw, int* status,
+                                   cudaStream_t st);
 cudaError_t launch_kinetic(int64_t n, int nboxes, const int64_t* atom0, int maxc, const double* const V[3],
                            const int* meta, LJTable lj, double* keAtom, double* partial, double* boxKE,
                            cudaStream_t st);

@@ -70,15 +70,20 @@ constexpr int kRedoBlocks = 152;       // grid of the redo pass (1 per SM)
 // Passes of the mixed form's tile body: the first pass; the redo pass's two
 // kinds of tile, one whose large terms were left out (only those are summed
 // and added) and one that overflowed the first pass's capacity (computed in
-// full at the redo capacity, large terms in an FP32 side array).
-constexpr int kMain = 0, kRedoBig = 1, kRedoFull = 2;
+// full at the redo capacity, large terms in an FP32 side array).  Pair-list
+// mode: the list build (the first pass's enumeration at the list cutoff,
+// writing the tile's pairs instead of their forces), the forces from the
+// list, and the redo of a listed tile's large terms.
+constexpr int kMain = 0, kRedoBig = 1, kRedoFull = 2, kListBuild = 3, kList = 4, kListBig = 5;
 constexpr int kFullBit = 1 << 30;      // redo-list entry: tile | kFullBit for an overflowed tile
 constexpr int kSeg = 4;                // lanes per segment of the i-side force sums
+constexpr int kMaxListK = 1024;        // pair-list mode: most list entries of one atom
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
   int lstart, gfirst, ox, oy, oz, dyt, dzt, img, cw, r2l, lut, ljt, queue;
   int pf, fa, px, code, fr;
+  int perm, hist;  // pair-list passes: the staged atoms by entry count, and the counts' histogram
   int bytes;
 };
 
@@ -97,10 +102,14 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
 // mode: kMain, kRedoBig (fr: the large terms' FP32 sums, over the
 // accepted-pair queues, which that pass does not use, when they fit there)
-// or kRedoFull (fr after everything else).
+// or kRedoFull (fr after everything else); kListBuild (the per-warp tables
+// without queues); kList, kListBig (no queues, no ownership table: the queue
+// region holds only the scan and reduction scratch; kListBig's fr after
+// everything).
 // ne_max, ext_max: the largest tile's ext cells and ext extent on one axis.
 __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int ext_max, int nw, int mode,
                                               bool pack) {
+  const bool from_list = mode == kList || mode == kListBig;
   Layout L;
   int o = 0;
   L.lstart = o; o = align16(o + 2 * (ne_max + 1));  // < 2^16: at most the capacity
@@ -113,11 +122,13 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   L.img = o;    o = align16(o + (fp64 ? 3 * 32 : 0));  // periodic image per ext coordinate (FP64 form)
   L.cw = o;     o = align16(o + 16);  // unit counter, large-term flag, staged-atom total
   L.r2l = o;    o = align16(o + (fp64 ? 64 * nw : 0));  // rank -> lane tables (FP64 form)
-  L.lut = o;    o = align16(o + (int)sizeof(OwnLut));
+  L.lut = o;    o = align16(o + (from_list ? 0 : (int)sizeof(OwnLut)));
   // the LJ table per ordered type pair (several types): per-lane type indices
   // would serialise on the kernel-parameter bank, shared memory serves them at once
   L.ljt = o;    o = align16(o + (int)sizeof(LJ64) * EXAMD_MAX_TYPES * EXAMD_MAX_TYPES);
-  const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64 : 16 * kQueue + (pack ? kWarpTabCompact : kWarpTabWide)) * nw;
+  const int tab = pack ? kWarpTabCompact : kWarpTabWide;
+  const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64
+                           : (from_list ? 64 : (mode == kListBuild ? 0 : 16) * kQueue + tab)) * nw;
   L.queue = o;  o = align16(o + qbytes);
   L.pf = o;     o = align16(o + 16 * cap);
   if (fp64) {
@@ -128,8 +139,13 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
     L.px = o;
   }
   L.code = o;   o = align16(o + 2 * cap);
+  L.perm = L.hist = o;
+  if (from_list) {
+    L.perm = o; o = align16(o + 2 * cap);
+    L.hist = o; o = align16(o + 4 * (kMaxListK + 1));
+  }
   L.fr = L.queue;
-  if (!fp64 && (mode == kRedoFull || (mode == kRedoBig && 3 * 4 * cap > 16 * kQueue * nw))) {
+  if (!fp64 && (mode == kRedoFull || mode == kListBig || (mode == kRedoBig && 3 * 4 * cap > 16 * kQueue * nw))) {
     L.fr = o;   o = align16(o + 3 * 4 * cap);
   }
   L.bytes = o;
@@ -137,13 +153,30 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
 }
 
 static int redo_smem_bytes(const PairConfig& cfg, int cap_redo, int ne_max, int ext_max) {
-  return std::max(make_layout(false, cap_redo, ne_max, ext_max, cfg.warps, kRedoBig, cfg.pack).bytes,
-                  make_layout(false, cap_redo, ne_max, ext_max, cfg.warps, kRedoFull, cfg.pack).bytes);
+  const int b = std::max(make_layout(false, cap_redo, ne_max, ext_max, cfg.warps, kRedoBig, cfg.pack).bytes,
+                         make_layout(false, cap_redo, ne_max, ext_max, cfg.warps, kRedoFull, cfg.pack).bytes);
+  return cfg.list ? std::max(b, make_layout(false, cap_redo, ne_max, ext_max, cfg.warps, kListBig, cfg.pack).bytes)
+                  : b;
+}
+
+// The first pass's layout: the enumeration's, or in pair-list mode (without
+// counters, which the enumeration gives) the list pass's.
+static int main_smem_bytes(const PairConfig& cfg, int cap, int ne_max, int ext_max) {
+  const int mode = (cfg.list && !cfg.count && !cfg.fp64) ? kList : kMain;
+  return make_layout(cfg.fp64, cap, ne_max, ext_max, cfg.warps, mode, cfg.pack).bytes;
+}
+
+static int build_smem_bytes(const PairConfig& cfg, int cap, int ne_max, int ext_max) {
+  return make_layout(false, cap, ne_max, ext_max, cfg.warps, kListBuild, cfg.pack).bytes;
 }
 
 int pair_smem_bytes(const PairConfig& cfg, int cap, int cap_redo, int ne_max, int ext_max) {
-  const int main = make_layout(cfg.fp64, cap, ne_max, ext_max, cfg.warps, kMain, cfg.pack).bytes;
-  return cfg.fp64 ? main : std::max(main, redo_smem_bytes(cfg, cap_redo, ne_max, ext_max));
+  int b = make_layout(cfg.fp64, cap, ne_max, ext_max, cfg.warps, kMain, cfg.pack).bytes;
+  if (cfg.fp64) return b;
+  b = std::max(b, redo_smem_bytes(cfg, cap_redo, ne_max, ext_max));
+  if (cfg.list) b = std::max(b, std::max(main_smem_bytes(cfg, cap, ne_max, ext_max),
+                                         build_smem_bytes(cfg, cap, ne_max, ext_max)));
+  return b;
 }
 
 // Exact sum of FP32 terms in 64-bit fixed point (2^-32 resolution): the total
@@ -164,42 +197,22 @@ struct FixSum {
   }
 };
 
-// Forces of cnt queued accepted pairs, one per lane: entry = (d = x_j - x_i,
-// key) with key = i | j << 14 | type_i << 28 | type_j << 30; r^2 is recomputed
-// with the distance test's expression, so it has the same bits.  user_func.f90:58-69
-// in FP32: dg = -24 eps (2 s^12 - s^6) / r^2, f_i += dg d, f_j -= dg d.
-// The queue keeps an atom's accepted pairs next to each other, so the i-side
-// fixed-point terms are first summed over segments of each run of lanes with
-// the same i (a segmented shuffle scan; integer sums, so the result is exact)
-// and each segment's last lane adds its total: one shared atomic per segment
-// instead of one per pair on the same address.
-// A pair-force term too large for the fixed-point sums (|F| >= kFixMaxForce,
-// decided on r^2 < r2big of the type pair: r < ~0.74 sigma at eps = 1, which
-// thermal configurations do not reach) is left out here and raises the
-// tile's flag (*big_flag); the redo pass adds it.  SIDE (the full redo pass):
-// such terms go to the FP32 side sums fr instead.
-template <bool MULTI, bool ENERGY, bool COUNT, bool SIDE, class QD, class FA, class FR>
-__device__ __forceinline__ void force_batch(int cnt, int qh, const QD& qd, FA& fa, FR& fr, int cap, const PairArgs& A,
-                                            const LJ32* ljs, FixSum& ek, FixSum& wk, int& nacc, int* big_flag) {
-  const LJTable& lj = A.lj;
+// The force of one accepted pair per lane (act), from registers: d = x_j -
+// x_i with d.w = r^2, P the type pair's parameters; i = -1 on a lane outside
+// the batch, which also ends any run of equal i.  Lanes that hold a pair
+// that was not accepted keep their i, add nothing, and do not break the run.
+template <bool ENERGY, bool COUNT, bool SIDE, class FA, class FR>
+__device__ __forceinline__ void pair_force32(bool act, int i, int m, float4 d, const LJ32& P, FA& fa, FR& fr,
+                                             int cap, const PairArgs& A, FixSum& ek, FixSum& wk, int& nacc,
+                                             int* big_flag) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const bool act = lane < cnt;
-  int i = -1, m = 0;
   float fx = 0.f, fy = 0.f, fz = 0.f;
   bool big = false;
   if (act) {
-    const int slot = (qh + lane) & (kQueue - 1);
-    float4 d = qd[slot];
-    const unsigned key = __float_as_uint(d.w);
-    d.w = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));  // r^2 exactly as the distance test computed it
-    i = key & 0x3fff;
-    m = (key >> 14) & 0x3fff;
-    LJ32 P = lj.p32[0];
-    if (MULTI) P = ljs[((key >> 28) & 3) * lj.nt + (key >> 30)];
     big = d.w < P.r2big;  // left to the redo pass
     float dg = 0.f, e = 0.f;
-    const int rv = pair_fn32<ENERGY>(lj.pot, d.w, P, dg, e);
+    const int rv = pair_fn32<ENERGY>(A.lj.pot, d.w, P, dg, e);
     if (rv == 0) {
       const float dgs = kFix * dg;
       fx = dgs * d.x;
@@ -235,9 +248,10 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const QD& qd, FA& f
       *big_flag = 1;
     }
   }
-  // i side: sum over runs of equal i (inactive lanes form one run with i = -1),
-  // in segments of kSeg lanes from the run's first one: each segment's last
-  // lane adds the segment's total (4: measured against 2, 8 and 16)
+  // i side: sum over runs of equal i (lanes outside the batch form one run
+  // with i = -1), in segments of kSeg lanes from the run's first one: each
+  // segment's last lane adds the segment's total (4: measured against 2, 8
+  // and 16)
   const int ip = __shfl_up_sync(FULL, i, 1);
   const unsigned hb = __ballot_sync(FULL, lane == 0 || ip != i);
   const int dist = (lane - (31 - __clz(hb & (FULL >> (31 - lane))))) & (kSeg - 1);
@@ -251,11 +265,45 @@ __device__ __forceinline__ void force_batch(int cnt, int qh, const QD& qd, FA& f
     }
   }
   const bool tail = lane == 31 || dist == kSeg - 1 || ((hb >> (lane + 1)) & 1u);
-  if (act && tail) {
+  if (i >= 0 && tail && (ix | iy | iz) != 0) {
     atomicAdd(&fa[i], ix);
     atomicAdd(&fa[cap + i], iy);
     atomicAdd(&fa[2 * cap + i], iz);
   }
+}
+
+// Forces of cnt queued accepted pairs, one per lane: entry = (d = x_j - x_i,
+// key) with key = i | j << 14 | type_i << 28 | type_j << 30; r^2 is recomputed
+// with the distance test's expression, so it has the same bits.  user_func.f90:58-69
+// in FP32: dg = -24 eps (2 s^12 - s^6) / r^2, f_i += dg d, f_j -= dg d.
+// The queue keeps an atom's accepted pairs next to each other, so the i-side
+// fixed-point terms are first summed over segments of each run of lanes with
+// the same i (a segmented shuffle scan; integer sums, so the result is exact)
+// and each segment's last lane adds its total: one shared atomic per segment
+// instead of one per pair on the same address.
+// A pair-force term too large for the fixed-point sums (|F| >= kFixMaxForce,
+// decided on r^2 < r2big of the type pair: r < ~0.74 sigma at eps = 1, which
+// thermal configurations do not reach) is left out here and raises the
+// tile's flag (*big_flag); the redo pass adds it.  SIDE (the full redo pass):
+// such terms go to the FP32 side sums fr instead.
+template <bool MULTI, bool ENERGY, bool COUNT, bool SIDE, class QD, class FA, class FR>
+__device__ __forceinline__ void force_batch(int cnt, int qh, const QD& qd, FA& fa, FR& fr, int cap, const PairArgs& A,
+                                            const LJ32* ljs, FixSum& ek, FixSum& wk, int& nacc, int* big_flag) {
+  const int lane = threadIdx.x & 31;
+  const bool act = lane < cnt;
+  int i = -1, m = 0;
+  float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+  LJ32 P = A.lj.p32[0];
+  if (act) {
+    const int slot = (qh + lane) & (kQueue - 1);
+    d = qd[slot];
+    const unsigned key = __float_as_uint(d.w);
+    d.w = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));  // r^2 exactly as the distance test computed it
+    i = key & 0x3fff;
+    m = (key >> 14) & 0x3fff;
+    if (MULTI) P = ljs[((key >> 28) & 3) * A.lj.nt + (key >> 30)];
+  }
+  pair_force32<ENERGY, COUNT, SIDE>(act, i, m, d, P, fa, fr, cap, A, ek, wk, nacc, big_flag);
 }
 
 // FP64 form: the reference's arithmetic for cnt queued pairs that passed the
@@ -314,6 +362,15 @@ __device__ __forceinline__ void force_batch64(int cnt, const QK& qk, const PD& p
 //   that the first pass wrote;
 // - kRedoFull: the whole tile at capacity A.cap_redo, large terms in FP32
 //   side sums, outputs, energy and counters written as the first pass would.
+// Pair-list mode:
+// - kListBuild: the first pass's enumeration at the list cutoff (rl2, with
+//   prune2_list), which writes the tile's accepted pairs as staged-index
+//   entries to its list instead of computing them; a tile over capacity or
+//   with more pairs than its list holds goes to the fallback list;
+// - kList: the tile's forces from its list, with the same per-pair FP32
+//   expressions as the first pass (the same bits when the atoms are where
+//   the list was built), outputs, energy and the large-term flag as there;
+// - kListBig: kRedoBig from the list.
 template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, int MODE, bool PACK>
 __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -325,7 +382,9 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   const int tx = t1.x, ty = t1.y, tz = t1.z;
   const int EX = tx + 2, EY = ty + 2, EZ = tz + 2;
   const int NE = EX * EY * EZ;
-  const int cap = MODE == kMain ? A.cap : A.cap_redo;
+  constexpr bool kFromList = MODE == kList || MODE == kListBig;
+  if (kFromList && MODE == kList && A.lcount[tile] < 0) return;  // a fallback tile: the redo pass computes it
+  const int cap = (MODE == kMain || MODE == kListBuild || MODE == kList) ? A.cap : A.cap_redo;
   const Layout L = make_layout(FP64, cap, A.ne_max, A.ext_max, nw, MODE, PACK);
   // shared-memory arrays (index-checked in the checked build)
   int* const st = A.status;
@@ -365,7 +424,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   {
     const uint4* src = reinterpret_cast<const uint4*>(&c_own);
     uint4* dst = reinterpret_cast<uint4*>(sown);
-    for (int k = tid; k < (int)(sizeof(OwnLut) / 16); k += blockDim.x) dst[k] = src[k];
+    if (!kFromList)
+      for (int k = tid; k < (int)(sizeof(OwnLut) / 16); k += blockDim.x) dst[k] = src[k];
     if (MULTI)
       for (int k = tid; k < A.lj.nt * A.lj.nt; k += blockDim.x) {
         if (FP64)
@@ -446,6 +506,13 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     __syncthreads();
   }
   const int total = cw[2];
+  if (MODE == kListBuild && (total > cap || total > A.lslots)) {  // no list: the redo pass enumerates it every step
+    if (tid == 0) {
+      A.lcount[tile] = -1;
+      A.fb[atomicAdd(&A.lw[LW_FBN], 1)] = tile;
+    }
+    return;
+  }
   if (!FP64 && MODE == kMain && total > cap) {  // the redo pass computes it at its capacity
     if (tid == 0) A.redo[atomicAdd(A.redo_n, 1)] = tile | kFullBit;
     return;
@@ -485,11 +552,15 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) fd[c * cap + t] = 0.0;
       } else {
-        pf[t] = make_float4(ox[lx] + u.x, u.y, u.z, u.w);
+        // from a list: the type and the ext-cell code in w (the list pass
+        // reads both atoms' rows from them)
+        pf[t] = make_float4(ox[lx] + u.x, u.y, u.z,
+                            kFromList ? __int_as_float((__float_as_int(u.w) & 3) | ((int)cc << 2)) : u.w);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          if (MODE != kMain) fr[c * cap + t] = 0.f;
-          if (MODE != kRedoBig) fa[c * cap + t] = 0;
+          if (MODE == kRedoBig || MODE == kRedoFull || MODE == kListBig) fr[c * cap + t] = 0.f;
+          // (list build: fa holds the atoms' entry counts)
+          if (MODE == kMain || MODE == kRedoFull || MODE == kList || MODE == kListBuild) fa[c * cap + t] = 0;
         }
       }
       code[t] = cc;
@@ -498,6 +569,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   int* big_flag = cw + 1;  // mixed form: a term was too large for the fixed-point sums
   if (tid == 0) {
     cw[0] = 0;  // work-unit counter
+    cw[3] = 0;  // list build: the tile's entries so far
     *big_flag = 0;
   }
   __syncthreads();
@@ -509,7 +581,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   int ncand = 0, neval = 0, nacc = 0;
   // per-warp queue of accepted pairs (mixed form: the separation and the key
   // in one 16-byte entry, r^2 recomputed from it; FP64 form: the key only)
-  constexpr int kQe = FP64 ? 4 : 16;  // bytes per queue entry
+  // bytes per queue entry (the list build writes its pairs to the lists directly)
+  constexpr int kQe = FP64 ? 4 : (MODE == kListBuild ? 0 : 16);
   auto qd = EXAMD_ARR(float4, (float4*)(smem + L.queue) + warp * kQueue, kQueue, st);
   auto qk = EXAMD_ARR(int, (int*)(smem + L.queue) + warp * kQueue, kQueue, st);
   // per-warp tables (kWarpTab*): one step's items (ptA, ptB) and, mixed
@@ -528,6 +601,18 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   auto r2l = EXAMD_ARR(unsigned char, smem + L.r2l + 64 * warp, FP64 ? 64 : 1, st);  // FP64 form: two rank -> lane tables of 32
   // ---- accepted pairs go to the warp's queue (a ring of kQueue entries);
   // their forces are computed in full batches of 32 ----
+  // list build: an accepted pair (i, m) is entry k of atom i (i's entries
+  // side by side, lk per atom), k from the atom's counter (fa); entries
+  // beyond lk are counted, not written (the tile then goes to the fallback
+  // list)
+  const size_t ltile = (size_t)tile * A.lslots;
+  auto list_add = [&](bool acc, int key) {
+    if (!acc) return;
+    const int i = key & 0x3fff, m = (key >> 14) & 0x3fff;
+    const int k = atomicAdd(&fa[i], 1);
+    if (k < A.lk)
+      A.list[EXAMD_IDX((ltile + i) * A.lk + k, (size_t)A.ntiles * A.lslots * A.lk, st)] = (unsigned short)m;
+  };
   auto enqueue = [&](bool acc, const float4& dq, int key) {
     const unsigned bal = __ballot_sync(FULL, acc);
     if (acc) {
@@ -638,11 +723,14 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int tj = __float_as_int(pj.w);
       const int kb = __float_as_int(a.w);
       if (COUNT && valid) ++neval;
-      const float thr = MULTI ? ljs32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2;
+      const float thr = MODE == kListBuild ? (MULTI ? ljs32[((kb >> 28) & 3) * A.lj.nt + tj].rl2 : q32.rl2)
+                                           : (MULTI ? ljs32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2);
       // disjoint bit fields: the sum is the OR, in one instruction
       const int key = (int)((unsigned)kb + ((unsigned)m << 14) + (MULTI ? (unsigned)tj << 30 : 0u));
       if (MODE == kRedoBig)
         redo_pair(valid && dq.w <= thr, dq, key);
+      else if (MODE == kListBuild)
+        list_add(valid && dq.w <= thr, key);
       else
         enqueue(valid && dq.w <= thr, dq, key);
     }
@@ -722,7 +810,121 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   };
 
   int* ucnt = cw;  // work-unit counter
-  if constexpr (!FP64) {
+  if constexpr (kFromList) {
+    // ---- forces from the tile's lists ----
+    // The staged atoms are first ordered by entry count, most first (a
+    // counting sort in shared memory), and a warp takes 32 consecutive atoms
+    // of that order, one per lane: its lanes then have about as many entries
+    // each, and few idle while the longest list runs out.  A lane reads its
+    // atom's entries eight at a time (one 16-byte load, the next eight
+    // loaded ahead).  Entry m of atom i is the pair (i, m).  The separation
+    // is formed as the first pass forms it: x in the tile frame, y and z from
+    // the atoms' cell offsets and the origin offset between their rows (read
+    // from the rows in the staged codes); the same bits when the atoms are
+    // where the lists were built.  Atom i's terms add up in registers (exact
+    // integer sums) and go to shared memory once; m's go at once.
+    const unsigned short* lst = A.list + ltile * A.lk;
+    const unsigned short* cnts = A.lcnt + ltile;
+    auto perm = EXAMD_ARR(unsigned short, smem + L.perm, cap, st);
+    auto hist = EXAMD_ARR(int, smem + L.hist, kMaxListK + 1, st);
+    const int lk = A.lk;
+    for (int c = tid; c <= lk; c += blockDim.x) hist[c] = 0;
+    __syncthreads();
+    for (int t = tid; t < total; t += blockDim.x) atomicAdd(&hist[cnts[t]], 1);
+    __syncthreads();
+    if (warp == 0) {  // exclusive scan from the largest count down
+      int run = 0;
+      for (int c0 = lk; c0 >= 0; c0 -= 32) {
+        const int c = c0 - lane;
+        const int h = c >= 0 ? hist[c] : 0;
+        int x = h;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL, x, o);
+          if (lane >= o) x += y;
+        }
+        if (c >= 0) hist[c] = run + x - h;
+        run += __shfl_sync(FULL, x, 31);
+      }
+    }
+    __syncthreads();
+    for (int t = tid; t < total; t += blockDim.x) perm[atomicAdd(&hist[cnts[t]], 1)] = (unsigned short)t;
+    __syncthreads();
+    const int ng = (total + 31) >> 5;
+    while (true) {
+      int g = 0;
+      if (lane == 0) g = atomicAdd(ucnt, 1);
+      g = __shfl_sync(FULL, g, 0);
+      if (g >= ng) break;
+      const int r = g * 32 + lane;
+      const bool vi = r < total;
+      const int i = vi ? perm[r] : 0;
+      const int cnt = vi ? cnts[i] : 0;
+      const int gm = warp_max(cnt);
+      const float4 pi = pf[i];
+      const int wi = __float_as_int(pi.w);
+      const int ti = wi & 3;
+      const int lyi = (wi >> 7) & 31, lzi = (wi >> 12) & 31;
+      const int by = lyi * kDT + 2 - lyi, bz = lzi * kDT + 2 - lzi;  // + the j row: the row offset's entry
+      const uint4* row = reinterpret_cast<const uint4*>(lst + (size_t)i * lk);
+      auto eight = [&](int k) { return k < cnt ? __ldcs(row + (k >> 3)) : make_uint4(0u, 0u, 0u, 0u); };
+      uint4 nxt = eight(0);
+      int sx = 0, sy = 0, sz = 0;  // atom i's fixed-point sums
+      for (int k0 = 0; k0 < gm; k0 += 8) {
+        const uint4 cur = nxt;
+        nxt = eight(k0 + 8);
+        const unsigned wv[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const bool act = k0 + q < cnt;
+          const int m = act ? (int)((wv[q >> 1] >> (16 * (q & 1))) & 0xffffu) : 0;
+          const float4 pj = pf[m];
+          const int wj = __float_as_int(pj.w);
+          const float cy = dyt[by + ((wj >> 7) & 31)].x, cz = dzt[bz + ((wj >> 12) & 31)].x;
+          float4 dq;
+          dq.x = pj.x + (-pi.x);
+          dq.y = pj.y + (cy - pi.y);
+          dq.z = pj.z + (cz - pi.z);
+          dq.w = fmaf(dq.x, dq.x, fmaf(dq.y, dq.y, dq.z * dq.z));
+          const int tj = wj & 3;
+          const LJ32 P = MULTI ? ljs32[ti * A.lj.nt + tj] : q32;
+          const bool acc = act && dq.w <= P.rc2;
+          if (MODE == kListBig) {
+            redo_pair(acc, dq, i | (m << 14) | (ti << 28) | (tj << 30));
+          } else if (acc) {
+            float dg = 0.f, en = 0.f;
+            const int rv = pair_fn32<ENERGY>(A.lj.pot, dq.w, P, dg, en);
+            if (rv == 0) {
+              if (ENERGY) {
+                ek.add(en);
+                wk.add(-dg * dq.w);
+              }
+              if (dq.w < P.r2big) {
+                *big_flag = 1;  // left to the redo pass
+              } else {
+                const float dgs = kFix * dg;
+                const int ix = __float2int_rn(dgs * dq.x), iy = __float2int_rn(dgs * dq.y),
+                          iz = __float2int_rn(dgs * dq.z);
+                atomicAdd(&fa[m], -ix);
+                atomicAdd(&fa[cap + m], -iy);
+                atomicAdd(&fa[2 * cap + m], -iz);
+                sx += ix;
+                sy += iy;
+                sz += iz;
+              }
+            } else if (rv < 0) {
+              atomicOr(A.status, ST_PAIRFN);
+            }
+          }
+        }
+      }
+      if (MODE == kList && (sx | sy | sz) != 0) {
+        atomicAdd(&fa[i], sx);
+        atomicAdd(&fa[cap + i], sy);
+        atomicAdd(&fa[2 * cap + i], sz);
+      }
+    }
+  } else if constexpr (!FP64) {
     // ---- item building: (staged atom, owned row) pairs, laid end to end ----
     // A unit is 32 consecutive staged atoms and one of kParts shares of each
     // atom's list of owned rows (the rows whose ownership mask for the atom's
@@ -734,7 +936,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     // trimmed to those whose box comes within rc of the atom (the 1e-4 margin in
     // prune2 covers the FP32 rounding; the accepted pairs are unchanged).
     const int nunits = kParts * ((total + 31) >> 5);
-    const float prune2 = A.lj.prune2;
+    const float prune2 = MODE == kListBuild ? A.lj.prune2_list : A.lj.prune2;
     while (true) {
       int u = 0;
       if (lane == 0) u = atomicAdd(ucnt, 1);
@@ -963,7 +1165,29 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   }
   __syncthreads();
   // a large term was left out: list the tile for the redo pass
-  if (!FP64 && MODE == kMain && tid == 0 && *big_flag) A.redo[atomicAdd(A.redo_n, 1)] = tile;
+  if (!FP64 && (MODE == kMain || MODE == kList) && tid == 0 && *big_flag) A.redo[atomicAdd(A.redo_n, 1)] = tile;
+  if (MODE == kListBuild) {  // the atoms' entry counts; a tile with an atom over lk: the fallback list
+    int mx = 0;
+    for (int t = tid; t < total; t += blockDim.x) {
+      const int c = fa[t];
+      mx = max(mx, c);
+      A.lcnt[EXAMD_IDX(ltile + t, (size_t)A.lslots * A.ntiles, st)] = (unsigned short)min(c, A.lk);
+    }
+    mx = warp_max(mx);
+    if (lane == 0) atomicMax(&cw[3], mx);
+    __syncthreads();
+    if (tid == 0) {
+      const int n = cw[3];
+      atomicMax(&A.lw[LW_LMAX], n);
+      if (n > A.lk) {
+        A.lcount[tile] = -1;
+        A.fb[atomicAdd(&A.lw[LW_FBN], 1)] = tile;
+      } else {
+        A.lcount[tile] = total;
+      }
+    }
+    return;
+  }
 
   // (4) write-back: home atoms -> Fown, halo copies -> P[slot]
   for (int t = tid; t < total; t += blockDim.x) {
@@ -979,7 +1203,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       for (int c = 0; c < 3; ++c) F[EXAMD_IDX(c * A.N + g, 3 * A.N, st)] = fd[c * cap + t];
     } else {
       float4* F = slot == 0 ? (float4*)A.Fown : (float4*)A.P + (size_t)(slot - 1) * A.N;
-      if (MODE == kRedoBig) {
+      if (MODE == kRedoBig || MODE == kListBig) {
         // this copy's output was written by the first pass and by this tile
         // only (a copy's slot pattern is unique to one tile)
         const float x = fr[t], y = fr[cap + t], z = fr[2 * cap + t];
@@ -1067,17 +1291,37 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
   pair_tile<FP64, MULTI, ENERGY, COUNT, kMain, PACK>(A, A.order[blockIdx.x]);
 }
 
+// Pair-list mode: the forces of every tile from its list (fallback tiles
+// return at once: the redo pass enumerates them).
+template <bool MULTI, bool ENERGY>
+__global__ void __launch_bounds__(256, 4) k_pair_list(const PairArgs A) {
+  pair_tile<false, MULTI, ENERGY, false, kList, false>(A, A.order[blockIdx.x]);
+}
+
+// Pair-list mode: the lists of every tile, on the steps whose gate is set.
+template <bool MULTI, bool PACK>
+__global__ void __launch_bounds__(256, 4) k_pair_build(const PairArgs A) {
+  if (A.gate && !*A.gate) return;
+  pair_tile<false, MULTI, false, false, kListBuild, PACK>(A, A.order[blockIdx.x]);
+}
+
 // Mixed form: the redo pass over the tiles that k_pair listed (normally none,
 // and the blocks return at once).  The block that finishes last empties the
 // list: every block has read its length (a read that its loop and barrier
-// depend on) before its thread 0 counts the block done.
-template <bool MULTI, bool PACK, bool ENERGY, bool COUNT>
+// depend on) before its thread 0 counts the block done.  LIST (pair-list
+// mode): the listed tiles' large terms are redone from their lists, and the
+// fallback tiles (over capacity or with lists that did not fit when they were
+// built) are computed in full by enumeration, every step until the next build.
+template <bool MULTI, bool PACK, bool ENERGY, bool COUNT, bool LIST>
 __global__ void __launch_bounds__(256, 3) k_pair_redo(const PairArgs A) {
   const int n = *(volatile const int*)A.redo_n;
-  for (int j = blockIdx.x; j < n; j += gridDim.x) {
-    const int w = A.redo[j];
+  const int nfb = LIST ? *(volatile const int*)&A.lw[LW_FBN] : 0;
+  for (int j = blockIdx.x; j < n + nfb; j += gridDim.x) {
+    const int w = j < n ? A.redo[j] : (A.fb[j - n] | kFullBit);
     if (w & kFullBit)
       pair_tile<false, MULTI, ENERGY, COUNT, kRedoFull, PACK>(A, w & ~kFullBit);
+    else if (LIST)
+      pair_tile<false, MULTI, false, false, kListBig, PACK>(A, w);
     else
       pair_tile<false, MULTI, false, false, kRedoBig, PACK>(A, w);
     __syncthreads();
@@ -1096,8 +1340,8 @@ static void* kfn() {
   return (void*)&k_pair<FP64, MULTI, ENERGY, COUNT, PACK>;
 }
 
-// The FP64 form has one table layout (PACK = false).
-static void* pick(const PairConfig& c) {
+// The enumeration's first pass.  The FP64 form has one table layout (PACK = false).
+static void* pick_enum(const PairConfig& c) {
 #define EXAMD_PICK(F, M, P)                                            \
   if (c.energy && c.count) return kfn<F, M, true, true, P>();         \
   if (c.energy) return kfn<F, M, true, false, P>();                   \
@@ -1116,29 +1360,55 @@ static void* pick(const PairConfig& c) {
 #undef EXAMD_PICK
 }
 
-template <bool MULTI, bool PACK>
-static void* pick_redo_ec(const PairConfig& c) {
-  if (c.energy && c.count) return (void*)&k_pair_redo<MULTI, PACK, true, true>;
-  if (c.energy) return (void*)&k_pair_redo<MULTI, PACK, true, false>;
-  if (c.count) return (void*)&k_pair_redo<MULTI, PACK, false, true>;
-  return (void*)&k_pair_redo<MULTI, PACK, false, false>;
+// The first pass: in pair-list mode (the counters excepted, which the
+// enumeration counts) the list pass.
+static bool uses_list(const PairConfig& c) { return c.list && !c.fp64 && !c.count; }
+
+static void* pick(const PairConfig& c) {
+  if (uses_list(c)) {
+    if (c.multi) return c.energy ? (void*)&k_pair_list<true, true> : (void*)&k_pair_list<true, false>;
+    return c.energy ? (void*)&k_pair_list<false, true> : (void*)&k_pair_list<false, false>;
+  }
+  return pick_enum(c);
 }
 
-static void* pick_redo(const PairConfig& c) {
-  if (c.pack) return c.multi ? pick_redo_ec<true, true>(c) : pick_redo_ec<false, true>(c);
-  return c.multi ? pick_redo_ec<true, false>(c) : pick_redo_ec<false, false>(c);
+static void* pick_build(const PairConfig& c) {
+  if (c.pack) return c.multi ? (void*)&k_pair_build<true, true> : (void*)&k_pair_build<false, true>;
+  return c.multi ? (void*)&k_pair_build<true, false> : (void*)&k_pair_build<false, false>;
 }
+
+template <bool MULTI, bool PACK, bool LIST>
+static void* pick_redo_ec(const PairConfig& c) {
+  if (c.energy && c.count) return (void*)&k_pair_redo<MULTI, PACK, true, true, LIST>;
+  if (c.energy) return (void*)&k_pair_redo<MULTI, PACK, true, false, LIST>;
+  if (c.count) return (void*)&k_pair_redo<MULTI, PACK, false, true, LIST>;
+  return (void*)&k_pair_redo<MULTI, PACK, false, false, LIST>;
+}
+
+template <bool LIST>
+static void* pick_redo_l(const PairConfig& c) {
+  if (c.pack) return c.multi ? pick_redo_ec<true, true, LIST>(c) : pick_redo_ec<false, true, LIST>(c);
+  return c.multi ? pick_redo_ec<true, false, LIST>(c) : pick_redo_ec<false, false, LIST>(c);
+}
+
+static void* pick_redo(const PairConfig& c) { return uses_list(c) ? pick_redo_l<true>(c) : pick_redo_l<false>(c); }
 
 cudaError_t pair_prepare(const PairConfig& cfg, int smem_bytes) {
   cudaError_t e = cudaFuncSetAttribute(pick(cfg), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
   if (e != cudaSuccess || cfg.fp64) return e;
-  return cudaFuncSetAttribute(pick_redo(cfg), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  e = cudaFuncSetAttribute(pick_redo(cfg), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  if (e != cudaSuccess || !uses_list(cfg)) return e;
+  return cudaFuncSetAttribute(pick_build(cfg), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
 }
 
+// Occupancy of the enumeration's first pass (the pair-list mode's build uses
+// the same tables).
 int pair_blocks_per_sm(const PairConfig& cfg, int cap, int ne_max, int ext_max) {
-  const int smem = make_layout(cfg.fp64, cap, ne_max, ext_max, cfg.warps, kMain, cfg.pack).bytes;
+  PairConfig c = cfg;
+  c.list = false;
+  const int smem = make_layout(c.fp64, cap, ne_max, ext_max, c.warps, kMain, c.pack).bytes;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pick(cfg), 32 * cfg.warps, (size_t)smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pick_enum(c), 32 * c.warps, (size_t)smem) != cudaSuccess)
     return 0;
   return n;
 }
@@ -1147,8 +1417,8 @@ cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, in
   if (ntiles <= 0) return cudaSuccess;
   void* fn = pick(cfg);
   void* args[] = {(void*)&a};
-  // smem_bytes (the larger of the two passes' needs) bounds both launches
-  const int main_smem = make_layout(cfg.fp64, a.cap, a.ne_max, a.ext_max, cfg.warps, kMain, cfg.pack).bytes;
+  // smem_bytes (the larger of the passes' needs) bounds every launch
+  const int main_smem = main_smem_bytes(cfg, a.cap, a.ne_max, a.ext_max);
   if (main_smem > smem_bytes) return cudaErrorInvalidValue;
   cudaError_t e = cudaLaunchKernel(fn, dim3(ntiles), dim3(32 * cfg.warps), args, (size_t)main_smem, st);
   if (e != cudaSuccess || cfg.fp64) return e;
@@ -1157,6 +1427,14 @@ cudaError_t launch_pair(const PairConfig& cfg, const PairArgs& a, int ntiles, in
   if (redo_smem > smem_bytes) return cudaErrorInvalidValue;
   return cudaLaunchKernel(pick_redo(cfg), dim3(std::min(ntiles, kRedoBlocks)), dim3(32 * cfg.warps), args,
                           (size_t)redo_smem, st);
+}
+
+cudaError_t launch_pair_build(const PairConfig& cfg, const PairArgs& a, int ntiles, int smem_bytes, cudaStream_t st) {
+  if (ntiles <= 0) return cudaSuccess;
+  void* args[] = {(void*)&a};
+  const int smem = build_smem_bytes(cfg, a.cap, a.ne_max, a.ext_max);
+  if (smem > smem_bytes) return cudaErrorInvalidValue;
+  return cudaLaunchKernel(pick_build(cfg), dim3(ntiles), dim3(32 * cfg.warps), args, (size_t)smem, st);
 }
 
 }  // namespace examd

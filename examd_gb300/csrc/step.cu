@@ -23,6 +23,60 @@ __device__ __forceinline__ void bin_store(int s, double x, double y, double z, c
   slot[s] = atomicAdd(&count[gc], 1);
 }
 
+// Pair-list mode.  Between two builds an atom keeps the cell it was sorted
+// into; its FP32 offset is taken from that cell's origin, so it may leave the
+// cell's range by up to half the skin.
+
+// x rounded to the nearest float, either sign, on the integer pipe.
+__device__ __forceinline__ float d2f_rn_signed(double x) {
+  const long long b = __double_as_longlong(x);
+  const float m = d2f_rn_nonneg(__longlong_as_double(b & 0x7fffffffffffffffll));
+  return b < 0 ? -m : m;
+}
+
+// The periodic image of an atom that crossed the box boundary since the
+// build, seen from its build cell (rare: out of line, so that its FP64
+// instructions are not run speculatively by every thread).
+static __device__ __noinline__ double offset_wrapped(double u, double L) { return u > 0.0 ? u - L : u + L; }
+
+// Offset of coordinate x (in [0, L)) from the origin of cell c on axis a,
+// rounded once to FP32: x - c*bl is exact (both are within a factor of two,
+// or c = 0), and an atom that crossed the periodic boundary is taken at its
+// image nearest the cell (it moved less than half the skin).
+__device__ __forceinline__ float list_offset(double x, int c, const BoxDev& B, int a) {
+  double u = x - mul_pow2((unsigned)(c * B.blq), B.blk);
+  const long long b = __double_as_longlong(u) & 0x7fffffffffffffffll;
+  if (d2f_trunc(__longlong_as_double(b)) > 0.5f * B.Lf[a]) u = offset_wrapped(u, B.L[a]);
+  return d2f_rn_signed(u);
+}
+
+// The list-mode offsets of one atom from its build cell (global cell gc),
+// and its squared displacement since the build (from the offsets Ub then).
+__device__ __forceinline__ float list_update(int64_t s, const double x[3], int gc, int type, const BoxDev& B,
+                                             float4* __restrict__ U, const float4* __restrict__ Ub) {
+  const int cl = gc - B.cell0;
+  const int q = cl / B.nb[0];
+  const int cx = cl - q * B.nb[0];
+  const int cz = q / B.nb[1];
+  const int cy = q - cz * B.nb[1];
+  float4 u;
+  u.x = list_offset(x[0], cx, B, 0);
+  u.y = list_offset(x[1], cy, B, 1);
+  u.z = list_offset(x[2], cz, B, 2);
+  u.w = __int_as_float(type);
+  U[s] = u;
+  const float4 b = Ub[s];
+  const float dx = u.x - b.x, dy = u.y - b.y, dz = u.z - b.z;
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// The warp's largest squared displacement into lw[LW_DISP] (non-negative
+// floats order as their bit patterns).  Every lane of the warp calls it.
+__device__ __forceinline__ void disp_max(float d2, int* lw) {
+  const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+  if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(&lw[LW_DISP], (int)m);
+}
+
 // Sum of an atom's force partials: the owning tile's, then the halo slots in
 // increasing order (fixed order: deterministic).  Mixed form: Kahan in FP32.
 __device__ __forceinline__ void gather_force(const StepArgs& a, int64_t s, double f[3]) {
@@ -198,7 +252,9 @@ cudaError_t launch_reduce_atoms(int nboxes, const int64_t* atom0, const double* 
 }
 
 // v += ckick F/m; optional kinetic energy at v + hk F/m; optional drift
-// x += dt v with periodic wrap followed by the binning count of the next step.
+// x += dt v with periodic wrap followed by the binning count of the next step
+// (pair-list mode: by the offsets from the build cells and the displacement
+// since the build instead).
 __global__ void k_kick(const KickArgs k) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool in = s < k.s.N;
@@ -222,26 +278,75 @@ __global__ void k_kick(const KickArgs k) {
     ke *= 0.5 * k.lj.mass[type];
     if (in) k.keAtom[s] = ke;
   }
-  if (!in) return;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    v[a] = v[a] + ck * f[a];
-    k.V[a][s] = v[a];
-  }
-  if (k.drift) {
-    const BoxDev& B = k.s.boxes[box];
-    double x[3];
+  float d2 = 0.f;  // pair-list mode: squared displacement since the build
+  if (in) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      x[a] = wrap_coord(fma(k.dt, v[a], k.X[a][s]), B.L[a], B.Li[a]);
-      k.X[a][s] = x[a];
+      v[a] = v[a] + ck * f[a];
+      k.V[a][s] = v[a];
     }
-    if (!(finite_bits(x[0]) && finite_bits(x[1]) && finite_bits(x[2]))) {
-      atomicOr(k.status, ST_NONFINITE);
-      x[0] = x[1] = x[2] = 0.0;
+    if (k.drift) {
+      const BoxDev& B = k.s.boxes[box];
+      double x[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        x[a] = wrap_coord(fma(k.dt, v[a], k.X[a][s]), B.L[a], B.Li[a]);
+        k.X[a][s] = x[a];
+      }
+      if (!(finite_bits(x[0]) && finite_bits(x[1]) && finite_bits(x[2]))) {
+        atomicOr(k.status, ST_NONFINITE);
+        x[0] = x[1] = x[2] = 0.0;
+      }
+      if (k.list)
+        d2 = list_update(s, x, k.s.cellS[s], type, B, k.U, k.Ub);
+      else
+        bin_store((int)s, x[0], x[1], x[2], B, k.cellOld, k.slot, k.count, k.s.nc, k.status);
     }
-    bin_store((int)s, x[0], x[1], x[2], B, k.cellOld, k.slot, k.count, k.s.nc, k.status);
   }
+  if (k.list && k.drift) disp_max(d2, k.lw);
+}
+
+// Pair-list mode: new positions for the caller's atoms [i0, i1) (AoS, caller
+// order): wrap, store at the sorted slot inv[i], offsets from the build cell
+// and the displacement since the build.
+__global__ void k_gather_pos_list(int64_t i0, int64_t i1, const double* __restrict__ aos,
+                                  const BoxDev* __restrict__ boxes, int strict, double* __restrict__ X0,
+                                  double* __restrict__ X1, double* __restrict__ X2, const int* __restrict__ meta,
+                                  const int* __restrict__ inv, const int* __restrict__ cellS, float4* __restrict__ U,
+                                  const float4* __restrict__ Ub, int* __restrict__ lw, int* __restrict__ status) {
+  const int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  float d2 = 0.f;
+  if (i < i1) {
+    const int s = inv[i];
+    const int mt = meta[s];
+    const BoxDev& B = boxes[mt >> 8];
+    double p[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      double x = aos[3 * i + a];
+      if (strict && !in_range_bits(x, B.L[a])) atomicOr(status, ST_OUTSIDE);
+      p[a] = finite_bits(x) ? wrap_coord(x, B.L[a], B.Li[a]) : x;
+    }
+    X0[s] = p[0];
+    X1[s] = p[1];
+    X2[s] = p[2];
+    if (!(finite_bits(p[0]) && finite_bits(p[1]) && finite_bits(p[2]))) {
+      atomicOr(status, ST_NONFINITE);
+      p[0] = p[1] = p[2] = 0.0;
+    }
+    d2 = list_update(s, p, cellS[s], mt & 0xff, B, U, Ub);
+  }
+  disp_max(d2, lw);
+}
+
+cudaError_t launch_gather_pos_list(int64_t i0, int64_t i1, const double* aos, const BoxDev* boxes, int strict,
+                                   double* X0, double* X1, double* X2, const int* meta, const int* inv,
+                                   const int* cellS, float4* U, const float4* Ub, int* lw, int* status,
+                                   cudaStream_t st) {
+  if (i1 <= i0) return cudaSuccess;
+  k_gather_pos_list<<<(unsigned)((i1 - i0 + 255) / 256), 256, 0, st>>>(i0, i1, aos, boxes, strict, X0, X1, X2, meta,
+                                                                       inv, cellS, U, Ub, lw, status);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_kick(const KickArgs& k, cudaStream_t st) {

@@ -20,7 +20,10 @@
 // keeps the 63-entry table exact, and a smaller one would break it.
 //
 // Each candidate gets its own context on the caller's atoms; the pair kernel
-// is timed with CUDA events (one warm-up launch, then kReps launches).  A
+// is timed with CUDA events (one warm-up launch, then kReps launches; in
+// pair-list mode the kernel that computes the forces from the lists, which
+// runs at every step, while the build runs only at the steps that rebuild).
+// With pair lists the reference's edge is (rc + skin) / 2.  A
 // candidate that does not fit (capacity, memory, fewer than 5 cells on an
 // axis) is skipped.  Choices can be kept in a text cache keyed by device,
 // precision, types, cutoff, box count, atom count and density.
@@ -50,10 +53,12 @@ std::string cache_key(const examd_params& p, int nboxes, const examd_box* boxes,
   for (int b = 0; b < nboxes; ++b) vol += boxes[b].L[0] * boxes[b].L[1] * boxes[b].L[2];
   for (int k = 0; k < p.ntypes * p.ntypes; ++k) rcmax = std::fmax(rcmax, p.rc[k]);
   char buf[256];
-  // atom count in quarter-octaves, density to 0.05; "ce": choices that include the cell edge
-  std::snprintf(buf, sizeof buf, "%s|%s|nt%d|rc%.4g|boxes%d|n%.2f|rho%.2f|ce", dev.c_str(),
+  // atom count in quarter-octaves, density to 0.05; "ce": choices that include the cell edge; the pair
+  // lists' skin
+  std::snprintf(buf, sizeof buf, "%s|%s|nt%d|rc%.4g|boxes%d|n%.2f|rho%.2f|ce|sk%.4g", dev.c_str(),
                 p.precision == EXAMD_FP64 ? "fp64" : "mixed", p.ntypes, rcmax, nboxes,
-                std::round(std::log2((double)(n > 0 ? n : 1)) * 4.0) / 4.0, std::round(n / vol * 20.0) / 20.0);
+                std::round(std::log2((double)(n > 0 ? n : 1)) * 4.0) / 4.0, std::round(n / vol * 20.0) / 20.0,
+                p.pair_skin);
   return buf;
 }
 
@@ -102,7 +107,7 @@ void cache_store(const char* path, const std::string& key, const int tile[3], in
 bool has_wide_cell(const examd_params& p, int nboxes, const examd_box* boxes) {
   double rcmax = 0.0;
   for (int k = 0; k < p.ntypes * p.ntypes; ++k) rcmax = std::fmax(rcmax, p.rc[k]);
-  const double bl = p.cell_edge > 0 ? p.cell_edge : 0.5 * rcmax;
+  const double bl = p.cell_edge > 0 ? p.cell_edge : 0.5 * (rcmax + p.pair_skin);
   if (!(bl > 0)) return false;
   for (int b = 0; b < nboxes; ++b)
     for (int a = 0; a < 3; ++a) {
@@ -167,7 +172,7 @@ extern "C" int examd_autotune(const examd_params* params, int nboxes, const exam
   std::stable_sort(done.begin(), done.end(), [](const Cand& x, const Cand& y) { return x.t < y.t; });
   double rcmax = 0.0;
   for (int k = 0; k < params->ntypes * params->ntypes; ++k) rcmax = std::fmax(rcmax, params->rc[k]);
-  const double edge0 = params->cell_edge > 0 ? params->cell_edge : 0.5 * rcmax;
+  const double edge0 = params->cell_edge > 0 ? params->cell_edge : 0.5 * (rcmax + params->pair_skin);
   const size_t ntop = std::min<size_t>(4, done.size());
   for (double scale : {1.1, 1.2})
     for (size_t k = 0; k < ntop; ++k) {

@@ -62,6 +62,8 @@ Module examd_gpu_mod
      Integer(c_int) :: potential
      Integer(c_int) :: pair_tables
      Integer(c_int) :: tile_balance
+     Real(c_double) :: pair_skin
+     Integer(c_int) :: pair_list_capacity
   End Type examd_params
 
   ! struct examd_box
@@ -151,6 +153,14 @@ Module examd_gpu_mod
        Real(c_double), Value :: dt
        Real(c_double), Intent(out) :: ms(3)
      End Function examd_gpu_time_phases
+
+     Integer(c_int) Function examd_gpu_list_info(ctx, builds, capacity, longest, fallback_tiles) &
+          bind(C, name="examd_gpu_list_info")
+       Import :: c_int, c_int64_t, c_ptr
+       Type(c_ptr), Value :: ctx
+       Integer(c_int64_t), Intent(out) :: builds
+       Integer(c_int), Intent(out) :: capacity, longest, fallback_tiles
+     End Function examd_gpu_list_info
 
      Integer(c_int) Function examd_gpu_get_state(ctx, pos, vel) bind(C, name="examd_gpu_get_state")
        Import :: c_int, c_ptr

@@ -96,6 +96,22 @@ typedef struct examd_params {
                       /* box's remainder) is >= 1.5 edges wide it counts as   */
                       /* two, so its tile has one cell fewer and the largest  */
                       /* tile, which sizes shared memory, is smaller          */
+  /* pair_skin: 0 = the reference's schedule, cells and candidate pairs
+   * rebuilt at every force evaluation.  > 0 (EXAMD_MIXED only): pair-list
+   * mode.  Each tile keeps the list of its pairs within rc + pair_skin, built
+   * by the same midpoint ownership; later evaluations compute the forces from
+   * the lists, and the cells and lists are rebuilt, on the device, at the
+   * first evaluation at which some atom has moved more than pair_skin / 2
+   * (less 1e-4) since the last build.  Every pair within rc is still
+   * computed exactly once, with the same FP32 expression.  The cell edge
+   * becomes at least (max(rc) + pair_skin) / 2. */
+  double pair_skin;
+  /* pair_list_capacity: pair-list mode's list entries per atom (the pairs it
+   * owns in its tile), a multiple of 8 up to 1024; 0 = sized by the library
+   * (the most at the first build + 20 %, grown when an atom outgrows it).  A
+   * tile with an atom whose pairs do not fit is computed by enumeration at
+   * every evaluation until the next build. */
+  int pair_list_capacity;
 } examd_params;
 
 /* One independent periodic box of a batched ensemble. */
@@ -144,7 +160,8 @@ int examd_gpu_forces(examd_ctx *ctx, double *forces, double *epot,
 int examd_gpu_forces_at(examd_ctx *ctx, const double *pos, double *forces,
                         double *epot, double *virial, int accumulate);
 
-/* nsteps velocity-Verlet steps of size dt (rebinning every step).  When
+/* nsteps velocity-Verlet steps of size dt (rebinning every step; in
+ * pair-list mode at the steps that rebuild the lists).  When
  * graph_chunk > 0 the step loop is captured once as a CUDA graph of
  * graph_chunk steps and replayed.  energies: when non-NULL, per-box
  * (ekin, epot) pairs after every step: nsteps * nboxes * 2 doubles. */
@@ -169,6 +186,14 @@ int examd_gpu_prepare_run(examd_ctx *ctx, double dt, int graph_chunk,
  * advance the state but are not a velocity-Verlet trajectory from a state
  * that examd_gpu_run left at full step: for timing only. */
 int examd_gpu_time_phases(examd_ctx *ctx, int nsteps, double dt, double *ms);
+
+/* Pair-list mode's state (zeros without it): the builds since the context
+ * was created, the list entries per atom, the most entries of one atom at
+ * the builds since the last call, and the tiles computed by enumeration
+ * because an atom's list did not fit or they outgrew the staged-atom
+ * capacity (until the next build). */
+int examd_gpu_list_info(examd_ctx *ctx, int64_t *builds, int *capacity,
+                        int *longest, int *fallback_tiles);
 
 /* Current positions and velocities in the caller's order (3*n each, NULL to
  * skip). */

@@ -46,7 +46,8 @@ def test_tuned_choice_cached_and_equivalent(gpulib, tmp_path, precision, tol):
 def test_cache_hit_needs_no_device(gpulib, tmp_path):
     """A cached choice is returned without timing (so without a device): tile,
     warps, tile split and cell edge come from the cache line; entries written
-    before the cell edge was tuned (no "|ce" key) are not used."""
+    before the cell edge was tuned (no "|ce" key) or before the pair lists'
+    skin entered the key (no "|sk") are not used."""
     from examd_gb300 import _lib
     L = np.array([107.49, 107.49, 107.49])
     n = 1048576
@@ -68,8 +69,10 @@ def test_cache_hit_needs_no_device(gpulib, tmp_path):
     cache = tmp_path / "tune.txt"
     cache.write_text(f"{key}|5 5 5 8 0.5\n"                 # old formats: ignored
                      f"{key}|tb|6 6 6 8 0.41 1\n"
-                     f"{key}|ce|5 4 4 4 0.42 0 0\n"
-                     f"{key}|ce|6 6 5 8 0.40 1 1.375\n")    # the last entry wins
+                     f"{key}|ce|6 6 6 4 0.30 1 0\n"
+                     f"{key}|ce|sk0|5 4 4 4 0.42 0 0\n"
+                     f"{key}|ce|sk0|6 6 5 8 0.40 1 1.375\n"  # the last entry wins
+                     f"{key}|ce|sk0.3|6 6 6 8 0.20 1 0\n")  # another skin
     best = _lib.Params()
     ms = C.c_double()
     pos = np.zeros((n, 3))
