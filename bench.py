@@ -18,9 +18,14 @@ steps, then K timed steps.
 
 value: atom-steps/s of the mixed form with all state resident in HBM, device
 time (CUDA events on the library's stream, the step loop replayed as CUDA
-graphs captured before the timed region), max over ranks.  e2e: the same
-metric through the drop-in force call with host buffers (pinned positions in,
-forces out, every step).  The line also carries the pair kernel's roofline,
+graphs captured before the timed region), max over ranks.  The mixed form
+runs with per-tile pair lists (skin 0.3 sigma, --pair-skin; 0 for cells and
+candidates at every step): a step computes its forces from the lists, and
+the cells and lists are rebuilt at the steps whose atoms moved more than half
+the skin, inside the timed steps.  e2e: the same metric through the drop-in
+force call with host buffers (pinned positions in, forces out, every call;
+the positions of consecutive steps in turn).  The line also carries the pair
+kernel's roofline,
 per-phase times, the CPU baseline (the oracle on the machine's host cores), and,
 on a separately equilibrated state, the FP64 form's rate at its own tuned
 tiles, the mixed form's force error against it and both forms' energy drift.
@@ -72,6 +77,9 @@ WORKLOADS = {
                    dt=0.005, eq=0, every=0, settle=100, drift=1000),
 }
 DEFAULT_WORKLOAD = "mixture"
+# the mixed form's pair lists: pairs within rc + 0.3 sigma, rebuilt when an
+# atom has moved 0.15 sigma since the last build
+PAIR_SKIN = 0.3
 
 
 def load_workloads():
@@ -184,10 +192,13 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def read_traffic(workload):
+def read_traffic(workload, lists=False):
     """DRAM bytes per pair-kernel launch from the committed ncu summary of this workload, if any."""
     names = {"mixture": ("pair_mixed_mixture_2097152.md", "traffic_bytes_per_launch_16777216"),
              "liquid": ("pair_mixed_fcc64_1048576.md", "traffic_bytes_per_launch")}
+    if lists:
+        names = {"mixture": ("pair_list_mixture_2097152.md", "traffic_bytes_per_launch_16777216"),
+                 "liquid": ("pair_list_liquid_1048576.md", "traffic_bytes_per_launch")}
     if workload not in names:
         return None, None
     fname, key = names[workload]
@@ -394,6 +405,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 / drift side measurements")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-tune", action="store_true", help="default tile shape instead of the autotuner's")
+    ap.add_argument("--pair-skin", type=float, default=PAIR_SKIN,
+                    help="mixed form's pair-list skin in sigma (0: cells and candidates at every step)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rk, lr = dist_info()
@@ -412,33 +425,37 @@ def main():
     n = int(case["natoms"].sum())
     nboxes = len(case["natoms"])
     lj = dict(case["lj"])
-    tuning = {}
-    tune_info = {"tile": "default", "warps": "default", "tile_balance": 0}
+    skin = float(args.pair_skin)
+    tuning = {"pair_skin": skin}
+    edge0 = "(rc + skin)/2" if skin > 0 else "rc/2 (the reference's)"
+    tune_info = {"tile": "default", "warps": "default", "tile_balance": 0, "pair_skin": skin}
     if not args.no_tune:
-        # tile shape, warps per CTA and tile split for these atoms (examd_autotune)
+        # tile shape, warps per CTA, tile split and cell edge for these atoms (examd_autotune)
         t = ex.autotune(case["boxes"], case["natoms"], case["pos"], case["types"], precision="mixed", device=lr,
-                        **lj)
+                        pair_skin=skin, **lj)
         tuning = {"tile": t["tile"], "warps": t["warps"], "tile_balance": t["tile_balance"],
-                  "block_length": t["block_length"]}
+                  "block_length": t["block_length"], "pair_skin": skin}
         tune_info = {"tile": list(t["tile"]), "warps": t["warps"], "tile_balance": t["tile_balance"],
-                     "cell_edge": t["block_length"] or "rc/2 (the reference's)"}
+                     "cell_edge": t["block_length"] or edge0, "pair_skin": skin}
     sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **tuning, **lj)
     sysm.set_atoms(case["pos"], case["types"], case["vel"])
     sysm.run(args.warmup, dt)  # exactly W untimed steps
     chunk = max(2, args.chunk // 2 * 2)
     sysm.prepare_run(dt, chunk)  # capture the step-loop graph outside the timed region
 
+    b0 = sysm.list_info()["builds"]
     barrier(dist)
     with ClockSampler(lr) as clk:
         out = sysm.run(args.steps, dt, graph_chunk=chunk)
     barrier(dist)
     t_ms = allmax(dist, out["ms"])
     value = n * args.steps * ws / (t_ms * 1e-3)
+    builds = sysm.list_info()["builds"] - b0  # rebuilds of the cells and pair lists in the timed steps
 
     # pair-kernel roofline: algorithmic FLOPs per launch / event-timed duration.  The candidates are the
-    # reference's pair calls at its own cell edge rc/2 (exaMD.f90:56), whatever edge the autotuner picked
+    # reference's pair calls at its own cell edge rc/2 (exaMD.f90:56), whatever edge the run uses
     cnt = sysm.counters()
-    if tuning.get("block_length"):
+    if tuning.get("block_length") or skin > 0:
         pos_now, _ = sysm.state()
         with ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **lj) as s0:
             s0.set_atoms(pos_now, case["types"])
@@ -447,21 +464,31 @@ def main():
     peak, peak_src = fp32_peak()
     _, k_ms = sysm.time_forces(20)
     achieved = flops / (k_ms * 1e-3) / 1e12
-    traffic, traffic_src = read_traffic(args.workload)
+    traffic, traffic_src = read_traffic(args.workload, skin > 0)
+    rebuild_ms = sysm.time_rebuild(2) if skin > 0 else 0.0
 
-    # end to end through the drop-in force call with pinned host buffers
-    state, _ = sysm.state()
+    # end to end through the drop-in force call with pinned host buffers: the caller's positions of
+    # consecutive steps (a pair-list context rebuilds when they have moved far enough since its build),
+    # each call timed from the host with the host->device and device->host copies inside
+    nstate = min(max(args.steps // 2, 10), 10 if n <= 4_000_000 else 4)
+    states = []
+    for _ in range(nstate):
+        sysm.run(1, dt)
+        states.append(sysm.state()[0])
     hp = ex.pinned_empty((n, 3))
-    hp[:] = state
     hf = ex.pinned_empty((n, 3))
+    hp[:] = states[-1]
     sysm.forces_at(hp, out=hf)
-    sysm.forces_at(hp, out=hf)  # both parities captured
+    sysm.forces_at(hp, out=hf)  # the captured call, at both parities of the sort's double buffer
     e2e_steps = max(args.steps // 2, 10)
-    barrier(dist)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    t_e2e = 0.0
+    for k in range(e2e_steps):
+        hp[:] = states[k % nstate]
+        barrier(dist)
+        t0 = time.perf_counter()
         sysm.forces_at(hp, out=hf)
-    t_e2e = allmax(dist, time.perf_counter() - t0)
+        t_e2e += time.perf_counter() - t0
+    t_e2e = allmax(dist, t_e2e)
     e2e = n * e2e_steps * ws / t_e2e
     phases = sysm.time_phases(10, dt)  # advances the state: last
     sysm.close()
@@ -472,19 +499,31 @@ def main():
             "precision": "mixed", "tuning": {**tune_info, "graph_chunk": chunk},
             "clocks": clk.summary(),
             "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
-                    "call": "examd_gpu_forces_at (positions in, forces out, pinned host buffers)"},
-            # per step: kick+drift+bin count, 2 scan kernels, finalize, pair, redo pass; + the closing kick
-            "gpu_launches": 6 * args.steps + 1,
+                    "call": "examd_gpu_forces_at (positions in, forces out, pinned host buffers), "
+                            f"positions of {nstate} consecutive steps in turn, each call timed"},
+            # per step: kick+drift+bin count, 2 scan kernels, finalize, pair, redo pass (pair lists: kick, the
+            # rebuild decision, bin count, 2 scan kernels, finalize, copy-back and list build, which return at
+            # once on a step that does not rebuild, list pass, redo pass); + the closing kick
+            "gpu_launches": (10 if skin > 0 else 6) * args.steps + 1,
             "phases_ms_per_step": phases,
             # pair rates of the timed run (the counters of one force evaluation x steps / time)
             "pairs": {"interactions_per_s": cnt["accepted"] * args.steps * ws / (t_ms * 1e-3),
                       "candidates_per_s": cnt["candidates"] * args.steps * ws / (t_ms * 1e-3),
                       "kernel_interactions_per_s": cnt["accepted"] / (k_ms * 1e-3)},
-            "roofline": {"bound": "fp32", "kernel": "k_pair (mixed)", "achieved": achieved,
+            "roofline": {"bound": "fp32", "kernel": "k_pair_list (mixed, pair lists)" if skin > 0 else "k_pair (mixed)",
+                         "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "traffic": traffic, "traffic_source": traffic_src, "kernel_ms": k_ms,
                          "flops_per_launch": flops, "candidates": cnt["candidates"], "accepted": cnt["accepted"],
                          "peak_source": peak_src}}
+    if skin > 0:
+        # the pair work of a step with the rebuilds' share: the list pass plus the timed steps' rebuilds
+        per_step_ms = k_ms + rebuild_ms * builds / args.steps
+        line["pair_lists"] = {"skin": skin, "rebuilds_in_timed_steps": builds, "steps": args.steps,
+                              "list_pass_ms": k_ms, "rebuild_ms": rebuild_ms,
+                              "pair_ms_per_step_with_rebuilds": per_step_ms,
+                              "achieved_per_step_tflops": flops / (per_step_ms * 1e-3) / 1e12,
+                              "frac_per_step": flops / (per_step_ms * 1e-3) / 1e12 / peak}
     if ws == 1 and not args.no_accuracy:
         line.update(accuracy_and_drift(ex, case, w, lj, tuning, lr, dt))
     if rk == 0 and ws == 1 and not args.no_cpu:

@@ -100,6 +100,7 @@ def load():
             "examd_gpu_prepare_run": (C.c_int, [ctxp, C.c_double, C.c_int, C.c_int]),
             "examd_gpu_time_phases": (C.c_int, [ctxp, C.c_int, C.c_double, dp]),
             "examd_gpu_list_info": (C.c_int, [ctxp, i64p, ip, ip, ip]),
+            "examd_gpu_time_rebuild": (C.c_int, [ctxp, C.c_int, dp]),
             "examd_gpu_get_state": (C.c_int, [ctxp, dp, dp]),
             "examd_gpu_kinetic": (C.c_int, [ctxp, dp]),
             "examd_kinetic_static": (C.c_int, [C.c_int, C.c_int64, C.c_int, i64p, vp, vp, vp, vp, C.c_int, dp, dp,

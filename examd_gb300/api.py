@@ -241,11 +241,19 @@ class MidpointLJ:
                   "examd_gpu_prepare_run")
 
     def time_phases(self, nsteps, dt):
-        """Average device ms per step of (kick + drift + binning count, scan + scatter, pair kernels) over
-        nsteps eager steps; advances the state (timing only)."""
+        """Average device ms per step over nsteps eager steps of: the kick with drift (and the binning count,
+        or in pair-list mode the offsets and displacement since the build); the binning's scan and scatter
+        (pair-list mode: the rebuild decision and the rebuilds of the steps that had one); the pair kernels.
+        Advances the state (timing only)."""
         ms = np.zeros(3)
         self._chk(self._lib.examd_gpu_time_phases(self._ctx, int(nsteps), float(dt), _d(ms)), "examd_gpu_time_phases")
-        return {"kick_bin_count": float(ms[0]), "bin_scan_scatter": float(ms[1]), "pair": float(ms[2])}
+        return {"kick": float(ms[0]), "binning": float(ms[1]), "pair": float(ms[2])}
+
+    def time_rebuild(self, reps=3):
+        """Pair-list mode: device ms of one rebuild of the cells and lists at the current positions."""
+        ms = C.c_double()
+        self._chk(self._lib.examd_gpu_time_rebuild(self._ctx, int(reps), C.byref(ms)), "examd_gpu_time_rebuild")
+        return ms.value
 
     def list_info(self):
         """Pair-list mode: builds so far, list entries per atom, the most entries of one atom at the builds

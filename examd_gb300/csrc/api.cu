@@ -1678,6 +1678,25 @@ int examd_gpu_time_phases(examd_ctx* ctx, int nsteps, double dt, double* ms) {
   return EXAMD_OK;
 }
 
+int examd_gpu_time_rebuild(examd_ctx* ctx, int reps, double* ms) {
+  if (!ctx || reps < 1 || !ms) return EXAMD_ERR_ARG;
+  if (!ctx->list) return EXAMD_ERR_ARG;
+  if (!ctx->atoms_set) return EXAMD_ERR_STATE;
+  cudaSetDevice(ctx->dev);
+  CK(cudaEventRecord(ctx->e0, ctx->st));
+  for (int r = 0; r < reps; ++r) {
+    const int rc = rebuild(ctx, nullptr);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(ctx->e1, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, ctx->e0, ctx->e1));
+  *ms = t / reps;
+  ctx->forces_valid = false;  // the sorted order changed
+  return check_status(ctx);
+}
+
 int examd_gpu_list_info(examd_ctx* ctx, int64_t* builds, int* capacity, int* longest, int* fallback_tiles) {
   if (!ctx) return EXAMD_ERR_ARG;
   int64_t b = 0;

@@ -70,11 +70,21 @@ __device__ __forceinline__ float list_update(int64_t s, const double x[3], int g
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
-// The warp's largest squared displacement into lw[LW_DISP] (non-negative
-// floats order as their bit patterns).  Every lane of the warp calls it.
+// The block's largest squared displacement into lw[LW_DISP] (non-negative
+// floats order as their bit patterns).  Every thread of the block calls it.
+// One atomic per block at most, and none when the block's maximum is not
+// above the value already there: atomics on one word serialise in L2, and
+// one per warp cost a third of the kick at 16.8M atoms.
 __device__ __forceinline__ void disp_max(float d2, int* lw) {
+  __shared__ unsigned wmax[32];
   const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
-  if ((threadIdx.x & 31) == 0 && m != 0u) atomicMax(&lw[LW_DISP], (int)m);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) wmax[w] = m;
+  __syncthreads();
+  if (w == 0) {
+    const unsigned b = __reduce_max_sync(0xffffffffu, lane < (int)(blockDim.x >> 5) ? wmax[lane] : 0u);
+    if (lane == 0 && b != 0u && (int)b > *(volatile int*)&lw[LW_DISP]) atomicMax(&lw[LW_DISP], (int)b);
+  }
 }
 
 // Sum of an atom's force partials: the owning tile's, then the halo slots in

@@ -23,7 +23,8 @@
 // is timed with CUDA events (one warm-up launch, then kReps launches; in
 // pair-list mode the kernel that computes the forces from the lists, which
 // runs at every step, while the build runs only at the steps that rebuild).
-// With pair lists the reference's edge is (rc + skin) / 2.  A
+// With pair lists the reference's edge is (rc + skin) / 2, and a candidate's
+// score adds a fifth of the time of a rebuild of its cells and lists.  A
 // candidate that does not fit (capacity, memory, fewer than 5 cells on an
 // axis) is skipped.  Choices can be kept in a text cache keyed by device,
 // precision, types, cutoff, box count, atom count and density.
@@ -41,6 +42,9 @@
 namespace {
 
 constexpr int kReps = 3;
+// pair-list mode: steps per rebuild assumed in the score (a thermal liquid at
+// a skin of 0.3 sigma and the usual time steps rebuilds every 4 to 9 steps)
+constexpr double kStepsPerBuild = 5.0;
 
 std::string cache_key(const examd_params& p, int nboxes, const examd_box* boxes, int64_t n) {
   cudaDeviceProp pr;
@@ -147,6 +151,11 @@ extern "C" int examd_autotune(const examd_params* params, int nboxes, const exam
     int rc = examd_gpu_create(&p, nboxes, boxes, &ctx);
     if (rc == EXAMD_OK) rc = examd_gpu_set_atoms(ctx, n, pos, type, nullptr);
     if (rc == EXAMD_OK) rc = examd_gpu_time_forces(ctx, kReps, nullptr, t);
+    if (rc == EXAMD_OK && p.pair_skin > 0.0) {  // the score: a step's share of a rebuild too
+      double tb = 0.0;
+      rc = examd_gpu_time_rebuild(ctx, 2, &tb);
+      *t += tb / kStepsPerBuild;
+    }
     if (ctx) examd_gpu_destroy(ctx);
     return rc;
   };

@@ -154,6 +154,13 @@ Module examd_gpu_mod
        Real(c_double), Intent(out) :: ms(3)
      End Function examd_gpu_time_phases
 
+     Integer(c_int) Function examd_gpu_time_rebuild(ctx, reps, ms) bind(C, name="examd_gpu_time_rebuild")
+       Import :: c_int, c_double, c_ptr
+       Type(c_ptr), Value :: ctx
+       Integer(c_int), Value :: reps
+       Real(c_double), Intent(out) :: ms
+     End Function examd_gpu_time_rebuild
+
      Integer(c_int) Function examd_gpu_list_info(ctx, builds, capacity, longest, fallback_tiles) &
           bind(C, name="examd_gpu_list_info")
        Import :: c_int, c_int64_t, c_ptr

@@ -178,14 +178,22 @@ int examd_gpu_prepare_run(examd_ctx *ctx, double dt, int graph_chunk,
                           int energies);
 
 /* Device time of the step's phases, averaged over nsteps eager steps of size
- * dt: ms[0] the kick with drift, wrap and binning count; ms[1] the rest of
- * the binning (scan and scatter); ms[2] the pair kernel and the mixed form's
- * redo pass.  CUDA events on the context's stream around each phase (the
+ * dt: ms[0] the kick with drift, wrap and binning count (pair-list mode: the
+ * offsets and displacement since the build instead of the count); ms[1] the
+ * rest of the binning, scan and scatter (pair-list mode: the rebuild
+ * decision, and the binning and list build of the steps that rebuild);
+ * ms[2] the pair kernel and the mixed form's redo pass.  CUDA events on the context's stream around each phase (the
  * reference stamps its force call with MPI_WTIME, exaMD.f90:234-263).  The
  * steps use the merged kick of the captured loop (v += dt F/m), so they
  * advance the state but are not a velocity-Verlet trajectory from a state
  * that examd_gpu_run left at full step: for timing only. */
 int examd_gpu_time_phases(examd_ctx *ctx, int nsteps, double dt, double *ms);
+
+/* Pair-list mode: device time of reps rebuilds of the cells and the pair
+ * lists at the current positions (the work of a step whose atoms moved more
+ * than half the skin), in ms per rebuild; the forces are computed again at
+ * the next call that needs them.  EXAMD_ERR_ARG without pair lists. */
+int examd_gpu_time_rebuild(examd_ctx *ctx, int reps, double *ms);
 
 /* Pair-list mode's state (zeros without it): the builds since the context
  * was created, the list entries per atom, the most entries of one atom at
