@@ -211,6 +211,7 @@ struct examd_ctx {
   int* inv = nullptr;         // caller index -> sorted slot
   bool inv_valid = false;     // inv matches the current sorted order
   cudaStream_t st2 = nullptr;
+  cudaStream_t stc = nullptr;  // pair-list mode: captures the rebuild into a conditional node's body
   cudaEvent_t ev_io[3 * kIoChunks + 1] = {};
   int maxc_atoms = 1, maxc_tiles = 1;
   int ebuf_steps = 0;
@@ -303,6 +304,7 @@ void free_all(examd_ctx* ctx) {
   for (cudaEvent_t e : ctx->ev_io)
     if (e) cudaEventDestroy(e);
   if (ctx->st2) cudaStreamDestroy(ctx->st2);
+  if (ctx->stc) cudaStreamDestroy(ctx->stc);
   if (ctx->e0) cudaEventDestroy(ctx->e0);
   if (ctx->e1) cudaEventDestroy(ctx->e1);
   if (ctx->e2) cudaEventDestroy(ctx->e2);
@@ -718,7 +720,8 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     return EXAMD_ERR_NOMEM;
   }
   *ctx->h_status = 0;
-  bool io_ok = cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) == cudaSuccess;
+  bool io_ok = cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) == cudaSuccess &&
+               cudaStreamCreateWithFlags(&ctx->stc, cudaStreamNonBlocking) == cudaSuccess;
   for (cudaEvent_t& e : ctx->ev_io) io_ok = io_ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
   if (!io_ok) {
     free_all(ctx);
@@ -1007,22 +1010,22 @@ PairArgs pair_args(examd_ctx* ctx) {
 }
 
 // Pair-list mode: the lists of every tile at the current cells.  gate: a
-// device word that makes the build conditional (the step loop), or nullptr:
-// build now, with the fallback list emptied first.
-int build_lists(examd_ctx* ctx, const int* gate) {
-  if (!gate) {
-    CK(cudaMemsetAsync(ctx->lw + LW_FBN, 0, sizeof(int), ctx->st));
-    ++ctx->host_builds;
-  }
+// device word that makes the build conditional (eager steps), or nullptr:
+// build now, with the fallback list emptied first (host: a build the host
+// asked for, counted here; otherwise the body of a captured rebuild, which
+// the device counts).
+int build_lists(examd_ctx* ctx, const int* gate, bool host = true) {
+  if (!gate) CK(cudaMemsetAsync(ctx->lw + LW_FBN, 0, sizeof(int), ctx->st));
+  if (!gate && host) ++ctx->host_builds;
   PairArgs a = pair_args(ctx);
   a.gate = gate;
   CK(launch_pair_build(ctx->pc, a, ctx->ntiles, ctx->smem, ctx->st));
   return EXAMD_OK;
 }
 
-// Pair-list mode: cells and lists rebuilt at the current positions (gate as
-// for build_lists).
-int rebuild(examd_ctx* ctx, const int* gate) {
+// Pair-list mode: cells and lists rebuilt at the current positions (gate and
+// host as for build_lists).
+int rebuild(examd_ctx* ctx, const int* gate, bool host = true) {
   const int s = ctx->cur;
   if (ctx->N > 0) {
     k_bin_count<<<nblk(ctx->N), 256, 0, ctx->st>>>(ctx->N, ctx->X[s][0], ctx->X[s][1], ctx->X[s][2],
@@ -1031,16 +1034,54 @@ int rebuild(examd_ctx* ctx, const int* gate) {
     CK(cudaGetLastError());
   }
   const int rc = finish_binning(ctx, true, gate);
-  return rc ? rc : build_lists(ctx, gate);
+  return rc ? rc : build_lists(ctx, gate, host);
 }
 
 // Pair-list mode, after new positions: the device decides whether some atom
 // moved more than half the skin since the build (or a rebuild was asked
-// for), and the rebuild's kernels run or return at once on that decision.
+// for).  Eager, the rebuild's kernels run or return at once on that
+// decision.  Under stream capture (the step loop's graphs, the captured
+// force call) the rebuild is captured, ungated, as the body of a conditional
+// graph node whose value the decision sets, so a step without a rebuild
+// launches none of its kernels.
 int maybe_rebuild(examd_ctx* ctx) {
-  k_list_decide<<<1, 1, 0, ctx->st>>>(ctx->lw, ctx->disp_thr2);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(ctx->st, &cs));
+  if (cs != cudaStreamCaptureStatusActive) {
+    k_list_decide<<<1, 1, 0, ctx->st>>>(ctx->lw, ctx->disp_thr2, cudaGraphConditionalHandle{}, 0);
+    CK(cudaGetLastError());
+    return rebuild(ctx, ctx->lw + LW_GATE);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edges = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(ctx->st, &cs, nullptr, &g, &deps, &edges, &nd));
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+  k_list_decide<<<1, 1, 0, ctx->st>>>(ctx->lw, ctx->disp_thr2, h, 1);
   CK(cudaGetLastError());
-  return rebuild(ctx, ctx->lw + LW_GATE);
+  CK(cudaStreamGetCaptureInfo(ctx->st, &cs, nullptr, &g, &deps, &edges, &nd));
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeIf;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, deps, edges, nd, &np));
+  CK(cudaStreamUpdateCaptureDependencies(ctx->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  // the body: the rebuild's kernels, captured from a stream of their own
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(ctx->stc, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  cudaStream_t main = ctx->st;
+  ctx->st = ctx->stc;
+  const int rc = rebuild(ctx, nullptr, false);
+  ctx->st = main;
+  cudaGraph_t captured = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(ctx->stc, &captured);
+  if (rc) return rc;
+  if (ce != cudaSuccess) return ctx->cuda_fail(ce, "cudaStreamEndCapture (rebuild body)");
+  return EXAMD_OK;
 }
 
 // Pair-list mode: lists of `want` entries per staged atom, for the current

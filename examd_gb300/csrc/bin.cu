@@ -246,9 +246,12 @@ __global__ void k_copy_back(int64_t n, const double* __restrict__ Y0, const doub
 
 // Pair-list mode: one thread decides whether this step rebuilds and resets
 // the displacement maximum and the forced-rebuild request for the next step.
-// A rebuild empties the fallback list (the build fills it again).
-__global__ void k_list_decide(int* lw, float thr2) {
+// A rebuild empties the fallback list (the build fills it again).  Inside a
+// captured step loop the rebuild is the body of a conditional graph node,
+// whose value is set here: a step that does not rebuild launches none of it.
+__global__ void k_list_decide(int* lw, float thr2, cudaGraphConditionalHandle h, int cond) {
   const int rb = (__int_as_float(lw[LW_DISP]) > thr2 || lw[LW_FORCE] != 0) ? 1 : 0;
+  if (cond) cudaGraphSetConditional(h, (unsigned)rb);
   lw[LW_GATE] = rb;
   lw[LW_DISP] = 0;
   lw[LW_FORCE] = 0;

@@ -33,8 +33,10 @@ __global__ void k_copy_back(int64_t n, const double* Y0, const double* Y1, const
                             double* X1, double* X2, double* V0, double* V1, double* V2, int* meta, int* id,
                             const int* gate);
 // Pair-list mode: decide whether this step rebuilds (largest displacement
-// since the build against thr2 = (skin/2 - margin)^2, or a forced rebuild).
-__global__ void k_list_decide(int* lw, float thr2);
+// since the build against thr2 = (skin/2 - margin)^2, or a forced rebuild);
+// in a captured step loop (cond) also the value of the conditional graph
+// node that holds the rebuild.
+__global__ void k_list_decide(int* lw, float thr2, cudaGraphConditionalHandle h, int cond);
 constexpr int kScanTileHost = 2048;  // cells per scan block (kScanThreads * kScanItems)
 
 // ---- pair.cu ----------------------------------------------------------------
