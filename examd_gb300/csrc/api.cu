@@ -511,7 +511,11 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
     lj.p32[k].m24eps = (float)(-24.0 * e);
     lj.p32[k].c4eps = (float)(4.0 * e);
     lj.p32[k].rc2 = (float)(r * r);
-    lj.p32[k].rcut2 = (float)rcut2;
+    // the mixed form's own range test only where the potential ends inside
+    // rc (WCA); for the LJ forms the range is rc itself, which the candidate
+    // test decides, in FP64 at the border (an FP32 re-test there would drop
+    // a pair that the FP64 form applies)
+    lj.p32[k].rcut2 = p.potential == EXAMD_POT_WCA ? (float)rcut2 : INFINITY;
     lj.p32[k].eshift = (float)eshift;
     lj.p32[k].rl2 = (float)((r + skin) * (r + skin));
     {

@@ -98,7 +98,8 @@ struct BoxDev {
 
 // LJ parameters per ordered type pair, FP32 (mixed) and FP64.
 // rc2: the candidate cutoff (distance test, queue); rcut2: the potential's
-// own range (<= rc2); eshift: subtracted from the pair energy.
+// own range (<= rc2; FP32 table: infinite where it is rc2, which the
+// candidate test decides); eshift: subtracted from the pair energy.
 struct LJ32 {
   float sig2, m24eps, c4eps, rc2;  // m24eps = -24 eps (dg prefactor)
   float rcut2, eshift;

@@ -46,6 +46,10 @@
 
 #include <cuda_fp16.h>
 
+// The list build returns before the write-back that the other passes of the
+// same tile body run (its instantiation has that code unreachable, by design).
+#pragma nv_diag_suppress 128
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "pairfn.cuh"
@@ -78,6 +82,11 @@ constexpr int kMain = 0, kRedoBig = 1, kRedoFull = 2, kListBuild = 3, kList = 4,
 constexpr int kFullBit = 1 << 30;      // redo-list entry: tile | kFullBit for an overflowed tile
 constexpr int kSeg = 4;                // lanes per segment of the i-side force sums
 constexpr int kMaxListK = 1024;        // pair-list mode: most list entries of one atom
+// Mixed form: a pair whose FP32 r^2 lies within this fraction of rc^2 (a few
+// times the FP32 separation's rounding) is accepted or not on its FP64 r^2,
+// as the FP64 form decides it, so that no pair straddling the cutoff enters
+// one form's sums and not the other's (about 1e-4 of an atom's pairs)
+constexpr float kBorder = 4e-6f;
 
 // Shared-memory carve-up, identical on host and device.
 struct Layout {
@@ -387,7 +396,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   const int cap = (MODE == kMain || MODE == kListBuild || MODE == kList) ? A.cap : A.cap_redo;
   const Layout L = make_layout(FP64, cap, A.ne_max, A.ext_max, nw, MODE, PACK);
   // shared-memory arrays (index-checked in the checked build)
-  int* const st = A.status;
+  int* const st = A.status;  // the index checks' status word (checked build)
+  (void)st;
   auto lstart = EXAMD_ARR(unsigned short, smem + L.lstart, A.ne_max + 1, st);
   auto gfirst = EXAMD_ARR(int, smem + L.gfirst, A.ne_max, st);
   auto ox = EXAMD_ARR(float, smem + L.ox, A.ext_max + 1, st);
@@ -637,6 +647,28 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     }
   };
 
+  // ---- mixed form: the FP64 cutoff test of a pair of staged atoms (a, b)
+  // at the border, r^2 from the FP64 positions as the FP64 form and the
+  // reference form it: the difference, then the periodic image (the pair is
+  // far nearer than half a box), SRC/exaMD_forces.f90:509-523 ----
+  auto inside64 = [&](int a, int b, int ta, int tb) -> bool {
+    auto gidx = [&](int t) {
+      const int c = code[t];
+      const int e = (c & 31) + EX * (((c >> 5) & 31) + EY * (c >> 10));
+      return (int64_t)gfirst[e] + (t - (int)lstart[e]);
+    };
+    const int64_t ga = EXAMD_IDX(gidx(a), A.N, st), gb = EXAMD_IDX(gidx(b), A.N, st);
+    const double* Xs[3] = {A.X0, A.X1, A.X2};
+    double d2 = 0.0;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      double d = __dsub_rn(Xs[ax][gb], Xs[ax][ga]);
+      d = __dsub_rn(d, __dmul_rn(rint(__dmul_rn(d, B.Li[ax])), B.L[ax]));
+      d2 = ax == 0 ? __dmul_rn(d, d) : __dadd_rn(d2, __dmul_rn(d, d));
+    }
+    return d2 <= A.lj.p64[ta * A.lj.nt + tb].rc2;
+  };
+
   // ---- redo pass: the force of each accepted pair at once; only the large
   // terms, decided exactly as force_batch decides them, are summed (both atoms)
   auto redo_pair = [&](bool acc, const float4& dq, int key) {
@@ -727,12 +759,15 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
                                            : (MULTI ? ljs32[((kb >> 28) & 3) * A.lj.nt + tj].rc2 : q32.rc2);
       // disjoint bit fields: the sum is the OR, in one instruction
       const int key = (int)((unsigned)kb + ((unsigned)m << 14) + (MULTI ? (unsigned)tj << 30 : 0u));
+      bool acc = valid && dq.w <= thr;
+      if ((MODE == kMain || MODE == kRedoFull) && valid && fabsf(dq.w - thr) <= kBorder * thr)
+        acc = inside64(kb & 0x3fff, m, MULTI ? (kb >> 28) & 3 : 0, MULTI ? tj : 0);  // at the border: FP64
       if (MODE == kRedoBig)
-        redo_pair(valid && dq.w <= thr, dq, key);
+        redo_pair(acc, dq, key);
       else if (MODE == kListBuild)
-        list_add(valid && dq.w <= thr, key);
+        list_add(acc, key);
       else
-        enqueue(valid && dq.w <= thr, dq, key);
+        enqueue(acc, dq, key);
     }
     __syncwarp();
   };
@@ -888,7 +923,9 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
           dq.w = fmaf(dq.x, dq.x, fmaf(dq.y, dq.y, dq.z * dq.z));
           const int tj = wj & 3;
           const LJ32 P = MULTI ? ljs32[ti * A.lj.nt + tj] : q32;
-          const bool acc = act && dq.w <= P.rc2;
+          bool acc = act && dq.w <= P.rc2;
+          if (MODE == kList && act && fabsf(dq.w - P.rc2) <= kBorder * P.rc2)
+            acc = inside64(i, m, ti, tj);  // at the border: the FP64 test
           if (MODE == kListBig) {
             redo_pair(acc, dq, i | (m << 14) | (ti << 28) | (tj << 30));
           } else if (acc) {

@@ -226,6 +226,7 @@ def main(argv=None):
     ap.add_argument("--tile", type=int, nargs="+", default=None, help="tile edge, or edges per axis")
     ap.add_argument("--tile-balance", type=int, default=0, choices=[0, 1],
                     help="split of each axis into tiles: 0 by cell count, 1 by width")
+    ap.add_argument("--pair-skin", type=float, default=0.0, help="mixed form's pair-list skin (0: none)")
     a = ap.parse_args(argv)
     kw = {"liquid": {"nc": a.nc}, "fcc": {}, "slab": {"n": a.n}, "ensemble": {"nboxes": a.nboxes},
           "binary_mixture": {"m": a.m}}[a.case]
@@ -233,7 +234,7 @@ def main(argv=None):
     tile = None if a.tile is None else (a.tile * 3 if len(a.tile) == 1 else a.tile)
     if tile is not None and len(tile) != 3:
         ap.error("--tile takes one edge or three")
-    with system(case, a.precision, tile=tile, tile_balance=a.tile_balance) as s:
+    with system(case, a.precision, tile=tile, tile_balance=a.tile_balance, pair_skin=a.pair_skin) as s:
         for _ in range(a.evals):
             s.forces()
         cnt = s.counters()

@@ -189,3 +189,32 @@ def test_energy_conservation_like_the_enumeration(gpulib, liquid, melted):
         e = (r["ekin"] + r["epot"])[:, 0]
         drift.append(abs(e[-1] - e[0]) / abs(e[0]))
     assert drift[1] <= max(5 * drift[0], 2e-5)
+
+
+def test_pairs_at_the_cutoff_decided_as_the_fp64_form(gpulib):
+    """Isolated pairs at r = rc (1 + delta), |delta| <= 3e-7, where the FP32
+    r^2 and the FP64 one can fall on different sides of rc^2: the mixed form
+    (per-step enumeration and pair lists) decides each such pair on its FP64
+    r^2, so exactly the pairs the FP64 form applies have a force, and each
+    within two steps of the fixed-point sums (2^-16) of it."""
+    rng = np.random.default_rng(11)
+    L = 90.0
+    g = np.arange(10) * 9.0 + 1.0  # 9 apart: atoms of different pairs stay 4 apart at least
+    centers = np.stack(np.meshgrid(g, g, g[:2], indexing="ij"), -1).reshape(-1, 3)  # 200 pairs
+    u = rng.normal(size=centers.shape)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    r = 2.5 * (1.0 + rng.uniform(-3e-7, 3e-7, len(centers)))
+    pos = np.concatenate([centers, centers + u * r[:, None]])
+    box = [L, L, L]
+    with gpulib.MidpointLJ(box, [len(pos)], precision="fp64", rc=2.5) as d:
+        d.set_atoms(pos)
+        g64, _, _ = d.forces()
+    on64 = np.linalg.norm(g64, axis=1) > 0
+    assert 0 < on64.sum() < len(pos)  # both sides of the cutoff are present
+    for skin in (0.0, SKIN):
+        with gpulib.MidpointLJ(box, [len(pos)], precision="mixed", rc=2.5, pair_skin=skin) as s:
+            s.set_atoms(pos)
+            f, _, _ = s.forces()
+        on = np.linalg.norm(f, axis=1) > 0
+        assert np.array_equal(on, on64)
+        assert np.abs(f[on] - g64[on]).max() <= 2.0 ** -16
