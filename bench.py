@@ -77,9 +77,11 @@ WORKLOADS = {
                    dt=0.005, eq=0, every=0, settle=100, drift=1000),
 }
 DEFAULT_WORKLOAD = "mixture"
-# the mixed form's pair lists: pairs within rc + 0.3 sigma, rebuilt when an
-# atom has moved 0.15 sigma since the last build
-PAIR_SKIN = 0.3
+# the mixed form's pair lists: the skin (pairs within rc + skin, rebuilt when
+# an atom has moved skin/2 since the last build) is picked among these by
+# short untimed runs of the workload's own dynamics (a larger skin rebuilds
+# less often and tests more pairs per step)
+PAIR_SKINS = (0.3, 0.4, 0.5)
 
 
 def load_workloads():
@@ -405,8 +407,9 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 / drift side measurements")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-tune", action="store_true", help="default tile shape instead of the autotuner's")
-    ap.add_argument("--pair-skin", type=float, default=PAIR_SKIN,
-                    help="mixed form's pair-list skin in sigma (0: cells and candidates at every step)")
+    ap.add_argument("--pair-skin", type=float, default=None,
+                    help="mixed form's pair-list skin in sigma (0: cells and candidates at every step; "
+                         "default: picked among 0.3, 0.4, 0.5)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rk, lr = dist_info()
@@ -425,7 +428,7 @@ def main():
     n = int(case["natoms"].sum())
     nboxes = len(case["natoms"])
     lj = dict(case["lj"])
-    skin = float(args.pair_skin)
+    skin = float(args.pair_skin) if args.pair_skin is not None else PAIR_SKINS[len(PAIR_SKINS) // 2]
     tuning = {"pair_skin": skin}
     edge0 = "(rc + skin)/2" if skin > 0 else "rc/2 (the reference's)"
     tune_info = {"tile": "default", "warps": "default", "tile_balance": 0, "pair_skin": skin}
@@ -437,6 +440,20 @@ def main():
                   "block_length": t["block_length"], "pair_skin": skin}
         tune_info = {"tile": list(t["tile"]), "warps": t["warps"], "tile_balance": t["tile_balance"],
                      "cell_edge": t["block_length"] or edge0, "pair_skin": skin}
+    if args.pair_skin is None and skin > 0:
+        # the skin: 20 steps from the workload's state at each candidate, the tiles above
+        trial = {}
+        for sk in PAIR_SKINS:
+            with ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr,
+                               **dict(tuning, pair_skin=sk), **lj) as s:
+                s.set_atoms(case["pos"], case["types"], case["vel"])
+                s.run(args.warmup, dt)
+                s.prepare_run(dt, 20)
+                trial[sk] = s.run(20, dt, graph_chunk=20)["ms"]
+        skin = min(trial, key=trial.get)
+        tuning["pair_skin"] = skin
+        tune_info["pair_skin"] = skin
+        tune_info["pair_skin_trials_ms_per_20_steps"] = {str(k): v for k, v in trial.items()}
     sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **tuning, **lj)
     sysm.set_atoms(case["pos"], case["types"], case["vel"])
     sysm.run(args.warmup, dt)  # exactly W untimed steps

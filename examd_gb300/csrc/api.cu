@@ -229,6 +229,8 @@ struct examd_ctx {
   float disp_thr2 = 0.f;  // rebuild when an atom moved more than this squared
   float4* Ub = nullptr;
   unsigned short* plist = nullptr;
+  unsigned short* plraw = nullptr;   // the build's scratch (each atom's entries in staged order)
+  unsigned short* plperm = nullptr;  // the staged atoms in the order of their entry counts
   unsigned short* plcnt = nullptr;
   int lk = 0, lslots = 0, list_gen = 0;
   int* lcount = nullptr;
@@ -287,7 +289,7 @@ void free_all(examd_ctx* ctx) {
                   ctx->Fown, ctx->P, ctx->tileE, ctx->tileW, ctx->tileC, ctx->boxE, ctx->boxW, ctx->boxKE,
                   ctx->status, ctx->d_occ, ctx->stage, ctx->stage2, ctx->d_meta_in, ctx->d_factor,
                   ctx->d_atom0, ctx->keAtom, ctx->partial, ctx->redo, ctx->redo_n,
-                  ctx->Ub, ctx->plist, ctx->plcnt, ctx->lcount, ctx->fb, ctx->lw};
+                  ctx->Ub, ctx->plist, ctx->plraw, ctx->plperm, ctx->plcnt, ctx->lcount, ctx->fb, ctx->lw};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (int b = 0; b < 2; ++b) {
@@ -1002,6 +1004,8 @@ PairArgs pair_args(examd_ctx* ctx) {
   a.redo_n = ctx->redo_n;
   a.redo_done = (unsigned*)(ctx->redo_n + 1);
   a.list = ctx->plist;
+  a.lraw = ctx->plraw;
+  a.lperm = ctx->plperm;
   a.lcnt = ctx->plcnt;
   a.lcount = ctx->lcount;
   a.lk = ctx->lk;
@@ -1095,16 +1099,16 @@ int set_list_capacity(examd_ctx* ctx, int want) {
   const int slots = (ctx->cap + 31) & ~31;
   if (want == ctx->lk && slots == ctx->lslots && ctx->plist) return EXAMD_OK;
   CK(cudaStreamSynchronize(ctx->st));
-  if (ctx->plist) cudaFree(ctx->plist);
-  if (ctx->plcnt) cudaFree(ctx->plcnt);
-  ctx->plist = nullptr;
-  ctx->plcnt = nullptr;
+  for (unsigned short** q : {&ctx->plist, &ctx->plraw, &ctx->plperm, &ctx->plcnt}) {
+    if (*q) cudaFree(*q);
+    *q = nullptr;
+  }
   ctx->lk = ctx->lslots = 0;
   const size_t atoms = (size_t)ctx->ntiles * (size_t)slots;
-  int rc = dalloc(ctx, &ctx->plist, atoms * (size_t)want);
-  if (rc) return rc;
-  rc = dalloc(ctx, &ctx->plcnt, atoms);
-  if (rc) return rc;
+  int rc;
+  if ((rc = dalloc(ctx, &ctx->plist, atoms * (size_t)want)) || (rc = dalloc(ctx, &ctx->plraw, atoms * (size_t)want)) ||
+      (rc = dalloc(ctx, &ctx->plperm, atoms)) || (rc = dalloc(ctx, &ctx->plcnt, atoms)))
+    return rc;
   ctx->lk = want;
   ctx->lslots = slots;
   ++ctx->list_gen;

@@ -66,14 +66,20 @@ struct PairArgs {
   int* redo;
   int* redo_n;
   unsigned* redo_done;
-  // pair-list mode: per tile and staged atom i (lslots slots, a multiple of
-  // 32), up to lk entries (a multiple of 8, at most 1024), the staged
-  // indices m of the pairs (i, m) that the tile owns within the list cutoff
-  // (list[tile][i][k]); their counts lcnt[tile][i]; per tile the staged
-  // atoms, or -1 when the tile is in the fallback list fb (computed by
-  // enumeration every step); the list words (ListWord); the build's gate
-  // (nullptr: build unconditionally)
+  // pair-list mode, per tile (lslots staged-atom slots, a multiple of 32, of
+  // up to lk entries each, lk a multiple of 8 and at most 1024): the staged
+  // atoms in the order of their entry counts, most first (lperm), and their
+  // counts in that order (lcnt); the entries, the staged indices m of the
+  // pairs (i, m) that the tile owns within the list cutoff, in that order by
+  // groups of 32 atoms, entries k..k+3 of the group's 32 atoms side by side
+  // (list[tile][p / 32][k / 4][p % 32][k % 4] for the atom at position p);
+  // the build's scratch, each atom's entries in staged order
+  // (lraw[tile][i][k]); per tile the staged atoms, or -1 when the tile is in
+  // the fallback list fb (computed by enumeration every step); the list
+  // words (ListWord); the build's gate (nullptr: build unconditionally)
   unsigned short* list;
+  unsigned short* lraw;
+  unsigned short* lperm;
   unsigned short* lcnt;
   int* lcount;
   int lk;

@@ -112,9 +112,9 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 // mode: kMain, kRedoBig (fr: the large terms' FP32 sums, over the
 // accepted-pair queues, which that pass does not use, when they fit there)
 // or kRedoFull (fr after everything else); kListBuild (the per-warp tables
-// without queues); kList, kListBig (no queues, no ownership table: the queue
-// region holds only the scan and reduction scratch; kListBig's fr after
-// everything).
+// without queues, the count order and its histogram); kList, kListBig (no
+// queues, no ownership table: the queue region holds only the scan and
+// reduction scratch; kListBig's fr after everything).
 // ne_max, ext_max: the largest tile's ext cells and ext extent on one axis.
 __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, int ext_max, int nw, int mode,
                                               bool pack) {
@@ -149,9 +149,15 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   }
   L.code = o;   o = align16(o + 2 * cap);
   L.perm = L.hist = o;
-  if (from_list) {
-    L.perm = o; o = align16(o + 2 * cap);
-    L.hist = o; o = align16(o + 4 * (kMaxListK + 1));
+  if (mode == kListBuild) {  // the build orders the atoms by entry count, at its end:
+    // in the per-warp tables' region, which the enumeration no longer uses then, if it fits
+    if (align16(2 * cap) + 4 * (kMaxListK + 1) <= qbytes) {
+      L.perm = L.queue;
+      L.hist = L.queue + align16(2 * cap);
+    } else {
+      L.perm = o; o = align16(o + 2 * cap);
+      L.hist = o; o = align16(o + 4 * (kMaxListK + 1));
+    }
   }
   L.fr = L.queue;
   if (!fp64 && (mode == kRedoFull || mode == kListBig || (mode == kRedoBig && 3 * 4 * cap > 16 * kQueue * nw))) {
@@ -611,17 +617,17 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   auto r2l = EXAMD_ARR(unsigned char, smem + L.r2l + 64 * warp, FP64 ? 64 : 1, st);  // FP64 form: two rank -> lane tables of 32
   // ---- accepted pairs go to the warp's queue (a ring of kQueue entries);
   // their forces are computed in full batches of 32 ----
-  // list build: an accepted pair (i, m) is entry k of atom i (i's entries
-  // side by side, lk per atom), k from the atom's counter (fa); entries
-  // beyond lk are counted, not written (the tile then goes to the fallback
-  // list)
+  // list build: an accepted pair (i, m) is entry k of atom i in the scratch
+  // (i's entries side by side, lk per atom), k from the atom's counter (fa);
+  // entries beyond lk are counted, not written (the tile then goes to the
+  // fallback list)
   const size_t ltile = (size_t)tile * A.lslots;
   auto list_add = [&](bool acc, int key) {
     if (!acc) return;
     const int i = key & 0x3fff, m = (key >> 14) & 0x3fff;
     const int k = atomicAdd(&fa[i], 1);
     if (k < A.lk)
-      A.list[EXAMD_IDX((ltile + i) * A.lk + k, (size_t)A.ntiles * A.lslots * A.lk, st)] = (unsigned short)m;
+      A.lraw[EXAMD_IDX((ltile + i) * A.lk + k, (size_t)A.ntiles * A.lslots * A.lk, st)] = (unsigned short)m;
   };
   auto enqueue = [&](bool acc, const float4& dq, int key) {
     const unsigned bal = __ballot_sync(FULL, acc);
@@ -847,44 +853,21 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   int* ucnt = cw;  // work-unit counter
   if constexpr (kFromList) {
     // ---- forces from the tile's lists ----
-    // The staged atoms are first ordered by entry count, most first (a
-    // counting sort in shared memory), and a warp takes 32 consecutive atoms
-    // of that order, one per lane: its lanes then have about as many entries
-    // each, and few idle while the longest list runs out.  A lane reads its
-    // atom's entries eight at a time (one 16-byte load, the next eight
-    // loaded ahead).  Entry m of atom i is the pair (i, m).  The separation
-    // is formed as the first pass forms it: x in the tile frame, y and z from
+    // The build ordered the staged atoms by entry count, most first; a warp
+    // takes 32 consecutive atoms of that order, one per lane, so its lanes
+    // have about as many entries each and few idle while the longest runs
+    // out.  A lane reads four entries at a time, the warp's 32 lanes' four
+    // side by side (one 256-byte load per warp), the next four loaded
+    // ahead.  Entry m of atom i is the pair (i, m).  The separation is
+    // formed as the first pass forms it: x in the tile frame, y and z from
     // the atoms' cell offsets and the origin offset between their rows (read
     // from the rows in the staged codes); the same bits when the atoms are
     // where the lists were built.  Atom i's terms add up in registers (exact
     // integer sums) and go to shared memory once; m's go at once.
-    const unsigned short* lst = A.list + ltile * A.lk;
-    const unsigned short* cnts = A.lcnt + ltile;
-    auto perm = EXAMD_ARR(unsigned short, smem + L.perm, cap, st);
-    auto hist = EXAMD_ARR(int, smem + L.hist, kMaxListK + 1, st);
     const int lk = A.lk;
-    for (int c = tid; c <= lk; c += blockDim.x) hist[c] = 0;
-    __syncthreads();
-    for (int t = tid; t < total; t += blockDim.x) atomicAdd(&hist[cnts[t]], 1);
-    __syncthreads();
-    if (warp == 0) {  // exclusive scan from the largest count down
-      int run = 0;
-      for (int c0 = lk; c0 >= 0; c0 -= 32) {
-        const int c = c0 - lane;
-        const int h = c >= 0 ? hist[c] : 0;
-        int x = h;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(FULL, x, o);
-          if (lane >= o) x += y;
-        }
-        if (c >= 0) hist[c] = run + x - h;
-        run += __shfl_sync(FULL, x, 31);
-      }
-    }
-    __syncthreads();
-    for (int t = tid; t < total; t += blockDim.x) perm[atomicAdd(&hist[cnts[t]], 1)] = (unsigned short)t;
-    __syncthreads();
+    const unsigned short* lst = A.list + ltile * lk;
+    const unsigned short* perm = A.lperm + ltile;
+    const unsigned short* cnts = A.lcnt + ltile;
     const int ng = (total + 31) >> 5;
     while (true) {
       int g = 0;
@@ -894,23 +877,24 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int r = g * 32 + lane;
       const bool vi = r < total;
       const int i = vi ? perm[r] : 0;
-      const int cnt = vi ? cnts[i] : 0;
-      const int gm = warp_max(cnt);
+      const int cnt = vi ? cnts[r] : 0;
+      const int gm = __shfl_sync(FULL, cnt, 0);  // the order puts the group's longest first
       const float4 pi = pf[i];
       const int wi = __float_as_int(pi.w);
       const int ti = wi & 3;
       const int lyi = (wi >> 7) & 31, lzi = (wi >> 12) & 31;
       const int by = lyi * kDT + 2 - lyi, bz = lzi * kDT + 2 - lzi;  // + the j row: the row offset's entry
-      const uint4* row = reinterpret_cast<const uint4*>(lst + (size_t)i * lk);
-      auto eight = [&](int k) { return k < cnt ? __ldcs(row + (k >> 3)) : make_uint4(0u, 0u, 0u, 0u); };
-      uint4 nxt = eight(0);
+      // entries k..k+3 of this lane: 8 bytes at brick k / 4 of the group
+      const uint2* col = reinterpret_cast<const uint2*>(lst + (size_t)g * 32 * lk) + lane;
+      auto four = [&](int k) { return k < cnt ? __ldcs(col + (size_t)(k >> 2) * 32) : make_uint2(0u, 0u); };
+      uint2 nxt = four(0);
       int sx = 0, sy = 0, sz = 0;  // atom i's fixed-point sums
-      for (int k0 = 0; k0 < gm; k0 += 8) {
-        const uint4 cur = nxt;
-        nxt = eight(k0 + 8);
-        const unsigned wv[4] = {cur.x, cur.y, cur.z, cur.w};
+      for (int k0 = 0; k0 < gm; k0 += 4) {
+        const uint2 cur = nxt;
+        nxt = four(k0 + 4);
+        const unsigned wv[2] = {cur.x, cur.y};
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
+        for (int q = 0; q < 4; ++q) {
           const bool act = k0 + q < cnt;
           const int m = act ? (int)((wv[q >> 1] >> (16 * (q & 1))) & 0xffffu) : 0;
           const float4 pj = pf[m];
@@ -1203,20 +1187,69 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   __syncthreads();
   // a large term was left out: list the tile for the redo pass
   if (!FP64 && (MODE == kMain || MODE == kList) && tid == 0 && *big_flag) A.redo[atomicAdd(A.redo_n, 1)] = tile;
-  if (MODE == kListBuild) {  // the atoms' entry counts; a tile with an atom over lk: the fallback list
+  if (MODE == kListBuild) {
+    // The atoms in the order of their entry counts, most first (a counting
+    // sort), and the entries moved from the scratch into that order; a tile
+    // with an atom over lk goes to the fallback list.
+    const int lk = A.lk;
+    auto perm = EXAMD_ARR(unsigned short, smem + L.perm, cap, st);
+    auto hist = EXAMD_ARR(int, smem + L.hist, kMaxListK + 1, st);
     int mx = 0;
+    for (int c = tid; c <= lk; c += blockDim.x) hist[c] = 0;
+    __syncthreads();
     for (int t = tid; t < total; t += blockDim.x) {
       const int c = fa[t];
       mx = max(mx, c);
-      A.lcnt[EXAMD_IDX(ltile + t, (size_t)A.lslots * A.ntiles, st)] = (unsigned short)min(c, A.lk);
+      atomicAdd(&hist[min(c, lk)], 1);
     }
     mx = warp_max(mx);
     if (lane == 0) atomicMax(&cw[3], mx);
     __syncthreads();
+    if (warp == 0) {  // exclusive scan from the largest count down
+      int run = 0;
+      for (int c0 = lk; c0 >= 0; c0 -= 32) {
+        const int c = c0 - lane;
+        const int h = c >= 0 ? hist[c] : 0;
+        int x = h;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL, x, o);
+          if (lane >= o) x += y;
+        }
+        if (c >= 0) hist[c] = run + x - h;
+        run += __shfl_sync(FULL, x, 31);
+      }
+    }
+    __syncthreads();
+    for (int t = tid; t < total; t += blockDim.x) perm[atomicAdd(&hist[min((int)fa[t], lk)], 1)] = (unsigned short)t;
+    __syncthreads();
+    // a lane moves its atom's entries eight at a time (16 bytes from the
+    // atom's scratch row, two 8-byte bricks that the warp's lanes store side
+    // by side); entries past the count in the last bricks are never read
+    const size_t nbrick = (size_t)A.ntiles * A.lslots * lk / 4;
+    const unsigned short* raw = A.lraw + ltile * lk;
+    for (int g = warp; g * 32 < total; g += nw) {
+      const int p = g * 32 + lane;
+      const int t = p < total ? perm[p] : 0;
+      const int c = p < total ? min((int)fa[t], lk) : 0;
+      A.lperm[EXAMD_IDX(ltile + p, (size_t)A.lslots * A.ntiles, st)] = (unsigned short)t;
+      A.lcnt[EXAMD_IDX(ltile + p, (size_t)A.lslots * A.ntiles, st)] = (unsigned short)c;
+      const int gm = __shfl_sync(FULL, c, 0);
+      const uint4* src = reinterpret_cast<const uint4*>(raw + (size_t)t * lk);
+      const size_t b0 = (ltile + (size_t)g * 32) * lk / 4 + lane;  // brick k / 4 of this lane: b0 + (k / 4) * 32
+      uint2* dst = reinterpret_cast<uint2*>(A.list);
+      for (int k0 = 0; k0 < gm; k0 += 8) {
+        if (k0 < c) {
+          const uint4 v = src[k0 >> 3];
+          dst[EXAMD_IDX(b0 + (size_t)(k0 >> 2) * 32, nbrick, st)] = make_uint2(v.x, v.y);
+          if (k0 + 4 < c) dst[EXAMD_IDX(b0 + (size_t)((k0 >> 2) + 1) * 32, nbrick, st)] = make_uint2(v.z, v.w);
+        }
+      }
+    }
     if (tid == 0) {
       const int n = cw[3];
       atomicMax(&A.lw[LW_LMAX], n);
-      if (n > A.lk) {
+      if (n > lk) {
         A.lcount[tile] = -1;
         A.fb[atomicAdd(&A.lw[LW_FBN], 1)] = tile;
       } else {
