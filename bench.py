@@ -78,10 +78,19 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "mixture"
 # the mixed form's pair lists: the skin (pairs within rc + skin, rebuilt when
-# an atom has moved skin/2 since the last build) is picked among these by
-# short untimed runs of the workload's own dynamics (a larger skin rebuilds
-# less often and tests more pairs per step)
-PAIR_SKINS = (0.3, 0.4, 0.5)
+# an atom has moved skin/2 since the last build; 0: no lists, cells and
+# candidates at every step) is picked among these by short untimed runs of
+# the workload's own dynamics (a larger skin rebuilds less often and tests
+# more pairs per step), among those whose cell edge (rc + skin)/2 leaves
+# every box at least 5 cells per axis
+PAIR_SKINS = (0.0, 0.3, 0.4, 0.5)
+
+
+def skins_allowed(case):
+    """The candidate skins whose cells of edge (rc + skin)/2 leave 5 per axis in every box."""
+    rc = np.max(case["lj"]["rc"])
+    lmin = float(np.min(case["boxes"]))
+    return [sk for sk in PAIR_SKINS if (rc + sk) / 2.0 * 1.001 * 5.0 <= lmin]
 
 
 def load_workloads():
@@ -428,7 +437,9 @@ def main():
     n = int(case["natoms"].sum())
     nboxes = len(case["natoms"])
     lj = dict(case["lj"])
-    skin = float(args.pair_skin) if args.pair_skin is not None else PAIR_SKINS[len(PAIR_SKINS) // 2]
+    cands = skins_allowed(case)
+    # the tiles are tuned at the middle candidate skin
+    skin = float(args.pair_skin) if args.pair_skin is not None else cands[(len(cands) - 1) // 2 + (len(cands) > 2)]
     tuning = {"pair_skin": skin}
     edge0 = "(rc + skin)/2" if skin > 0 else "rc/2 (the reference's)"
     tune_info = {"tile": "default", "warps": "default", "tile_balance": 0, "pair_skin": skin}
@@ -440,20 +451,22 @@ def main():
                   "block_length": t["block_length"], "pair_skin": skin}
         tune_info = {"tile": list(t["tile"]), "warps": t["warps"], "tile_balance": t["tile_balance"],
                      "cell_edge": t["block_length"] or edge0, "pair_skin": skin}
-    if args.pair_skin is None and skin > 0:
-        # the skin: 20 steps from the workload's state at each candidate, the tiles above
+    if args.pair_skin is None and len(cands) > 1:
+        # the skin: a short run from the workload's state at each candidate, the tiles above (long enough to
+        # hold several rebuilds: 20 steps for millions of atoms, 100 for smaller systems)
+        ntrial = 20 if n > 4_000_000 else 100
         trial = {}
-        for sk in PAIR_SKINS:
+        for sk in cands:
             with ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr,
                                **dict(tuning, pair_skin=sk), **lj) as s:
                 s.set_atoms(case["pos"], case["types"], case["vel"])
                 s.run(args.warmup, dt)
                 s.prepare_run(dt, 20)
-                trial[sk] = s.run(20, dt, graph_chunk=20)["ms"]
+                trial[sk] = s.run(ntrial, dt, graph_chunk=20)["ms"] / ntrial
         skin = min(trial, key=trial.get)
         tuning["pair_skin"] = skin
         tune_info["pair_skin"] = skin
-        tune_info["pair_skin_trials_ms_per_20_steps"] = {str(k): v for k, v in trial.items()}
+        tune_info["pair_skin_trials_ms_per_step"] = {str(k): v for k, v in trial.items()}
     sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **tuning, **lj)
     sysm.set_atoms(case["pos"], case["types"], case["vel"])
     sysm.run(args.warmup, dt)  # exactly W untimed steps
