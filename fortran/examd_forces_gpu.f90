@@ -11,6 +11,7 @@
 !!!!!   In exaMD.f90, after exaMD_setup_midpoint_interactions (:230):
 !!!!!
 !!!!!     Call exaMD_forces_gpu_setup(cutoff, EXAMD_FP64)      ! or EXAMD_MIXED
+!!!!!     (or, with pair lists: Call exaMD_forces_gpu_setup(cutoff, EXAMD_MIXED, 0.4_PRC))
 !!!!!
 !!!!!   and in place of the force call at exaMD.f90:247-251:
 !!!!!
@@ -105,10 +106,14 @@ Contains
   !!  LJ parameters of the driver's set-up (prmvdw(1,1:5) = eps, sigma, -, -,
   !!  rc: exaMD.f90:199-202), the reference's cell edge rc/2 (exaMD.f90:56),
   !!  and the current positions.  precision: EXAMD_FP64 (the reference's
-  !!  arithmetic) or EXAMD_MIXED.
-  Subroutine exaMD_forces_gpu_setup(cutoff, precision)
+  !!  arithmetic) or EXAMD_MIXED.  skin (optional, EXAMD_MIXED only): the
+  !!  per-tile pair lists' skin in sigma; the library rebuilds its cells and
+  !!  lists at the calls whose atoms moved more than half of it since the last
+  !!  build, and the cell edge becomes (rc + skin)/2.
+  Subroutine exaMD_forces_gpu_setup(cutoff, precision, skin)
     Real(kind=PRC), Intent(in) :: cutoff
     Integer(c_int), Intent(in) :: precision
+    Real(kind=PRC), Intent(in), Optional :: skin
     Type(examd_params) :: p, best
     Type(examd_box) :: box(1)
     Real(c_double) :: ms
@@ -120,6 +125,7 @@ Contains
     p%sigma(1) = Real(prmvdw(1,2), c_double)
     p%rc(1) = Real(cutoff, c_double)
     p%cell_edge = 0.0_c_double
+    If (Present(skin)) p%pair_skin = Real(skin, c_double)
     box(1)%L = Real(globalbox, c_double)
     natms_gpu = local_atoms()
     box(1)%natoms = natms_gpu
