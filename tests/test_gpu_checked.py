@@ -1,5 +1,6 @@
 """The checked build (-DEXAMD_CHECKED): every shared-memory and global index
-of the pair, binning-scatter and kick kernels is tested against its array;
+of the pair kernels (enumeration, list build and list pass), the
+binning-scatter and the kick is tested against its array;
 a failure sets a status bit (the access goes to element 0 instead) and the
 call returns EXAMD_ERR_CHECK, with no trap.  It stands in for a memory
 checker, which may not run on this GPU pool.
@@ -20,7 +21,7 @@ pytestmark = [pytest.mark.gpu]
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SMALL = ["tests/test_gpu_parity.py", "tests/test_gpu_golden.py", "tests/test_gpu_close_pairs.py",
          "tests/test_gpu_tables.py", "tests/test_gpu_potentials.py", "tests/test_gpu_io_graph.py",
-         "tests/test_gpu_tile_balance.py"]
+         "tests/test_gpu_tile_balance.py", "tests/test_gpu_pair_list.py"]
 
 
 @pytest.fixture(scope="module")
