@@ -108,9 +108,9 @@ struct LJ32 {
 };
 
 // Mixed form: pair-force magnitude at which a term leaves the fixed-point sums
-// (2^16 scale, int32) for the redo pass (r < ~0.74 sigma at eps = 1); every
-// component of a kept term is below 2^27 in fixed point, so a component's
-// int32 sum needs more than 16 near-maximal terms of one sign to overflow.
+// (2^17 scale, int32) for the redo pass (r < ~0.74 sigma at eps = 1); every
+// component of a kept term is below 2^28 in fixed point, so a component's
+// int32 sum needs more than 8 near-maximal terms of one sign to overflow.
 constexpr float kFixMaxForce = 2048.f;
 struct LJ64 {
   double sig2, eps24, eps4, rc2;   // as user_func.f90:58-59 computes them

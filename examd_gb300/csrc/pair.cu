@@ -26,14 +26,14 @@
 // shared-memory atomics (the FP64 form's bound) rarely hit one address.
 //
 // Accumulation.  Mixed form: each per-atom force component is an exact 32-bit
-// fixed-point sum in shared memory (scale 2^16, native integer atomics), so
+// fixed-point sum in shared memory (scale 2^17, native integer atomics), so
 // the result does not depend on the order of the terms and is reproducible
 // bit for bit.  A term of magnitude >= 2048 (r < 0.74 sigma at eps = 1) is
-// left out and flags the tile, so every fixed-point term is below 2^27 and a
-// component's sum could leave the int32 range only through more than 16
-// near-maximal terms of one sign on one atom, i.e. 16 neighbours within about
+// left out and flags the tile, so every fixed-point term is below 2^28 and a
+// component's sum could leave the int32 range only through more than 8
+// near-maximal terms of one sign on one atom, i.e. 8 neighbours within about
 // 0.75 sigma on one side, which no physical configuration has (the repulsive
-// cores of 16 such neighbours do not fit in one hemisphere).  A second
+// cores of 8 such neighbours do not fit in one hemisphere).  A second
 // launch (k_pair_redo) recomputes the flagged tiles, sums their large terms
 // in FP32 and adds them to the outputs; thermal configurations flag no tile
 // and the launch returns at once (only the rare FP32 sums' order can vary
@@ -63,13 +63,17 @@ cudaError_t upload_own_lut(const OwnLut& lut) { return cudaMemcpyToSymbol(c_own,
 constexpr int kDT = 6;        // origin differences for d = -2..3
 constexpr int kQueue = 64;    // per-warp queue of accepted pairs
 constexpr int kParts = 2;     // work units per 32 staged atoms (1, 3 and 4 measured slower)
-// Fixed-point scale 2^16: each term is rounded to 2^-17 in absolute value.
-// Measured on the 1M-atom liquid against the FP64 form (RMS of |dF_i| /
-// F_rms): 4.9e-6 at 2^15, 4.0e-6 at 2^16, 3.75e-6 at 2^17; the rest is the
-// FP32 rounding of the pair separations, which the steep repulsive core
-// amplifies.
-constexpr float kFix = 65536.f;
-constexpr float kFixInv = 1.f / 65536.f;
+// Fixed-point scale 2^17: each term is rounded to 2^-18 in absolute value.
+// With the pairs at the cutoff decided in FP64, the mixed form's error on an
+// equilibrated 1M-atom liquid was 2.38e-6 RMS of F_rms at 2^16, about 1.6e-6
+// of it the sums' rounding (55 terms an atom at F_rms ~ 35) and the rest the
+// FP32 separations; 2^17 halves the rounding share.  Every kept term is below
+// kFixMaxForce, so below 2^28 in fixed point: a component's int32 sum (exact
+// modulo 2^32 whatever the order) leaves the range only through more than 8
+// near-maximal terms of one sign on one atom, which no physical
+// configuration has.
+constexpr float kFix = 131072.f;
+constexpr float kFixInv = 1.f / 131072.f;
 constexpr int kRedoBlocks = 152;       // grid of the redo pass (1 per SM)
 // Passes of the mixed form's tile body: the first pass; the redo pass's two
 // kinds of tile, one whose large terms were left out (only those are summed
