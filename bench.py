@@ -463,10 +463,18 @@ def main():
                 s.run(args.warmup, dt)
                 s.prepare_run(dt, 20)
                 trial[sk] = s.run(ntrial, dt, graph_chunk=20)["ms"] / ntrial
+        tuned_at = skin
         skin = min(trial, key=trial.get)
         tuning["pair_skin"] = skin
         tune_info["pair_skin"] = skin
         tune_info["pair_skin_trials_ms_per_step"] = {str(k): v for k, v in trial.items()}
+        if skin != tuned_at and not args.no_tune:  # the tiles again, for the skin picked
+            t = ex.autotune(case["boxes"], case["natoms"], case["pos"], case["types"], precision="mixed",
+                            device=lr, pair_skin=skin, **lj)
+            tuning.update(tile=t["tile"], warps=t["warps"], tile_balance=t["tile_balance"],
+                          block_length=t["block_length"])
+            tune_info.update(tile=list(t["tile"]), warps=t["warps"], tile_balance=t["tile_balance"],
+                             cell_edge=t["block_length"] or ("(rc + skin)/2" if skin > 0 else "rc/2 (the reference's)"))
     sysm = ex.MidpointLJ(case["boxes"], case["natoms"], precision="mixed", device=lr, **tuning, **lj)
     sysm.set_atoms(case["pos"], case["types"], case["vel"])
     sysm.run(args.warmup, dt)  # exactly W untimed steps
