@@ -76,3 +76,40 @@ def test_graph_replay_with_energy_across_a_run(gpulib, case):
         s.run(6, 0.001, graph_chunk=4)  # grows the energy buffers again
         _, e, w = s.forces_at(hp, out=hf, energy=True)
         assert np.array_equal(hf, f_ref) and np.array_equal(e, e_ref) and np.array_equal(w, w_ref)
+
+
+def test_graph_replay_with_pair_lists(gpulib, case):
+    """Pair lists (mixed form): the captured force call holds the rebuild as
+    a conditional graph node.  Replays over positions that move a little
+    (no rebuild) and then past half the skin (a rebuild inside the graph)
+    equal the eager calls bit for bit, and the rebuilds happen where the
+    eager context has them.  The atoms move past half the skin by a common
+    shift: random moves that large bring pairs within 0.74 sigma, whose
+    large terms the redo pass sums in FP32 in an order that can vary
+    between runs."""
+    rng = np.random.default_rng(5)
+    L = case["boxes"][0]
+    shifts = [(0, 0, 0), (0, 0, 0), (0.2, 0.1, -0.05), (0.2, 0.1, -0.05), (0.42, 0.1, -0.05), (0.42, 0.1, -0.05)]
+    steps = [(case["pos"] + np.asarray(d) + rng.uniform(-0.02, 0.02, case["pos"].shape)) % L for d in shifts]
+    kw = dict(precision="mixed", pair_skin=0.3, **case["lj"])
+    eager, graph, b_e, b_g = [], [], [], []
+    with gpulib.MidpointLJ(case["boxes"], case["natoms"], **kw) as s:
+        s.set_atoms(case["pos"])
+        for p in steps:
+            f, e, w = s.forces_at(p, energy=True)
+            eager.append((f.copy(), e.copy(), w.copy()))
+            b_e.append(s.list_info()["builds"])
+    hp = gpulib.pinned_empty(case["pos"].shape)
+    hf = gpulib.pinned_empty(case["pos"].shape)
+    with gpulib.MidpointLJ(case["boxes"], case["natoms"], **kw) as s:
+        s.set_atoms(case["pos"])
+        for p in steps:
+            hp[:] = p
+            _, e, w = s.forces_at(hp, out=hf, energy=True)
+            graph.append((hf.copy(), e, w))
+            b_g.append(s.list_info()["builds"])
+    assert b_e == b_g
+    assert [b - b_e[0] for b in b_e] == [0, 0, 1, 1, 2, 2]
+    for (fa, ea, wa), (fb, eb, wb) in zip(eager, graph):
+        assert np.array_equal(fa, fb)
+        assert np.array_equal(ea, eb) and np.array_equal(wa, wb)

@@ -85,3 +85,29 @@ def test_wca_needs_rc_over_its_range(gpulib):
     with pytest.raises(_lib.ExamdError) as err:
         gpulib.MidpointLJ([10.0, 10.0, 10.0], [10], rc=1.0, block_length=1.25, potential="wca")
     assert err.value.code == _lib.ERR_ARG
+
+
+@pytest.mark.parametrize("pot", ["lj_shifted", "wca"])
+def test_pair_lists_with_other_potentials(gpulib, pot):
+    """The pair plug-in in pair-list mode: at the build the list pass gives
+    the enumeration's forces and energy bit for bit (same cell edge), and
+    after the atoms moved less than half the skin its forces stay within
+    1e-5 of an O(N^2) FP64 sum (WCA: pairs between 2^(1/6) sigma and rc are
+    in the lists and skipped by the pair function)."""
+    L = np.array([14.0, 15.0, 16.0])
+    pos = gpulib.gen_random(2000, L, 0.85, 12)
+    skin = 0.3
+    kw = dict(precision="mixed", rc=2.5, potential=pot, block_length=0.5 * (2.5 + skin))
+    out = []
+    for sk in (0.0, skin):
+        with gpulib.MidpointLJ(L, [len(pos)], pair_skin=sk, **kw) as s:
+            s.set_atoms(pos)
+            out.append(s.forces(energy=True))
+            if sk:
+                moved = (pos + np.random.default_rng(3).uniform(-0.05, 0.05, pos.shape)) % L
+                f, _, _ = s.forces_at(moved)
+                assert s.list_info()["builds"] == 1
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    rcut, eshift = (2.5, 4.0 * (0.4 ** 6) * (0.4 ** 6 - 1.0)) if pot == "lj_shifted" else (2.0 ** (1.0 / 6.0), -1.0)
+    ref_f, _ = brute_force(moved, L, rcut, eshift)
+    assert np.sqrt(((f - ref_f) ** 2).sum(1).mean()) / np.sqrt((ref_f * ref_f).sum(1).mean()) <= 1e-5
