@@ -63,6 +63,11 @@ cudaError_t upload_own_lut(const OwnLut& lut) { return cudaMemcpyToSymbol(c_own,
 constexpr int kDT = 6;        // origin differences for d = -2..3
 constexpr int kQueue = 64;    // per-warp queue of accepted pairs
 constexpr int kParts = 2;     // work units per 32 staged atoms (1, 3 and 4 measured slower)
+// Warps per CTA of the list build, whatever the other passes use: the build
+// needs one count word per atom where they keep three force sums, and in the
+// room 12 warps fit 3 CTAs on an SM at the tiles of a dense liquid (36 warps
+// against 24 with 8), to hide its shared-memory latency.
+constexpr int kBuildWarps = 12;
 // Fixed-point scale 2^17: each term is rounded to 2^-18 in absolute value.
 // With the pairs at the cutoff decided in FP64, the mixed form's error on an
 // equilibrated 1M-atom liquid was 2.38e-6 RMS of F_rms at 2^16, about 1.6e-6
@@ -148,7 +153,7 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
     L.fa = o;   o = align16(o + 3 * 8 * cap);  // FP64 force sums
     L.px = o;   o = align16(o + 3 * 8 * cap);  // FP64 positions
   } else {
-    L.fa = o;   o = align16(o + 3 * 4 * cap);  // fixed-point force sums
+    L.fa = o;   o = align16(o + (mode == kListBuild ? 1 : 3) * 4 * cap);  // fixed-point force sums (build: counts)
     L.px = o;
   }
   L.code = o;   o = align16(o + 2 * cap);
@@ -186,7 +191,7 @@ static int main_smem_bytes(const PairConfig& cfg, int cap, int ne_max, int ext_m
 }
 
 static int build_smem_bytes(const PairConfig& cfg, int cap, int ne_max, int ext_max) {
-  return make_layout(false, cap, ne_max, ext_max, cfg.warps, kListBuild, cfg.pack).bytes;
+  return make_layout(false, cap, ne_max, ext_max, kBuildWarps, kListBuild, cfg.pack).bytes;
 }
 
 int pair_smem_bytes(const PairConfig& cfg, int cap, int cap_redo, int ne_max, int ext_max) {
@@ -553,7 +558,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     return;
   }
   // (3) stage atoms, one thread per ext cell
-  auto fa = EXAMD_ARR(int, smem + L.fa, 3 * cap, st);
+  auto fa = EXAMD_ARR(int, smem + L.fa, (MODE == kListBuild ? 1 : 3) * cap, st);
   auto fr = EXAMD_ARR(float, smem + L.fr, 3 * cap, st);  // redo pass: FP32 sums of the large terms
   auto fd = EXAMD_ARR(double, smem + L.fa, 3 * cap, st);
   auto pd = EXAMD_ARR(double, smem + L.px, 3 * cap, st);
@@ -579,8 +584,9 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           if (MODE == kRedoBig || MODE == kRedoFull || MODE == kListBig) fr[c * cap + t] = 0.f;
-          // (list build: fa holds the atoms' entry counts)
-          if (MODE == kMain || MODE == kRedoFull || MODE == kList || MODE == kListBuild) fa[c * cap + t] = 0;
+          // (list build: fa holds the atoms' entry counts, one word each)
+          if (MODE == kMain || MODE == kRedoFull || MODE == kList || (MODE == kListBuild && c == 0))
+            fa[c * cap + t] = 0;
         }
       }
       code[t] = cc;
@@ -1374,7 +1380,7 @@ __global__ void __launch_bounds__(256, 4) k_pair_list(const PairArgs A) {
 
 // Pair-list mode: the lists of every tile, on the steps whose gate is set.
 template <bool MULTI, bool PACK>
-__global__ void __launch_bounds__(256, 4) k_pair_build(const PairArgs A) {
+__global__ void __launch_bounds__(32 * kBuildWarps, 3) k_pair_build(const PairArgs A) {
   if (A.gate && !*A.gate) return;
   pair_tile<false, MULTI, false, false, kListBuild, PACK>(A, A.order[blockIdx.x]);
 }
@@ -1508,7 +1514,7 @@ cudaError_t launch_pair_build(const PairConfig& cfg, const PairArgs& a, int ntil
   void* args[] = {(void*)&a};
   const int smem = build_smem_bytes(cfg, a.cap, a.ne_max, a.ext_max);
   if (smem > smem_bytes) return cudaErrorInvalidValue;
-  return cudaLaunchKernel(pick_build(cfg), dim3(ntiles), dim3(32 * cfg.warps), args, (size_t)smem, st);
+  return cudaLaunchKernel(pick_build(cfg), dim3(ntiles), dim3(32 * kBuildWarps), args, (size_t)smem, st);
 }
 
 }  // namespace examd
