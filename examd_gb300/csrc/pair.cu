@@ -1248,11 +1248,18 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const uint4* src = reinterpret_cast<const uint4*>(raw + (size_t)t * lk);
       const size_t b0 = (ltile + (size_t)g * 32) * lk / 4 + lane;  // brick k / 4 of this lane: b0 + (k / 4) * 32
       uint2* dst = reinterpret_cast<uint2*>(A.list);
-      for (int k0 = 0; k0 < gm; k0 += 8) {
-        if (k0 < c) {
-          const uint4 v = src[k0 >> 3];
-          dst[EXAMD_IDX(b0 + (size_t)(k0 >> 2) * 32, nbrick, st)] = make_uint2(v.x, v.y);
-          if (k0 + 4 < c) dst[EXAMD_IDX(b0 + (size_t)((k0 >> 2) + 1) * 32, nbrick, st)] = make_uint2(v.z, v.w);
+      // 32 entries a round: the four 16-byte reads issued before the stores
+      for (int k0 = 0; k0 < gm; k0 += 32) {
+        uint4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = k0 + 8 * u < c ? src[(k0 >> 3) + u] : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int k = k0 + 8 * u;
+          if (k < c) {
+            dst[EXAMD_IDX(b0 + (size_t)(k >> 2) * 32, nbrick, st)] = make_uint2(v[u].x, v[u].y);
+            if (k + 4 < c) dst[EXAMD_IDX(b0 + (size_t)((k >> 2) + 1) * 32, nbrick, st)] = make_uint2(v[u].z, v[u].w);
+          }
         }
       }
     }
