@@ -148,7 +148,7 @@ __host__ __device__ inline Layout make_layout(bool fp64, int cap, int ne_max, in
   const int qbytes = (fp64 ? 4 * kQueue + kWarpTabFp64
                            : (from_list ? 64 : (mode == kListBuild ? 0 : 16) * kQueue + tab)) * nw;
   L.queue = o;  o = align16(o + qbytes);
-  L.pf = o;     o = align16(o + 16 * cap);
+  L.pf = o;     o = align16(o + 16 * (from_list ? cap + 1 : cap));  // list passes: + the padding atom
   if (fp64) {
     L.fa = o;   o = align16(o + 3 * 8 * cap);  // FP64 force sums
     L.px = o;   o = align16(o + 3 * 8 * cap);  // FP64 positions
@@ -427,7 +427,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   const signed char* srows = &sown->rows[0][0];
   LJ32* ljs32 = (LJ32*)(smem + L.ljt);
   LJ64* ljs64 = (LJ64*)(smem + L.ljt);
-  auto pf = EXAMD_ARR(float4, smem + L.pf, cap, st);
+  auto pf = EXAMD_ARR(float4, smem + L.pf, kFromList ? cap + 1 : cap, st);
   auto code = EXAMD_ARR(unsigned short, smem + L.code, cap, st);
   auto U = EXAMD_ARR(const float4, A.U, A.N, st);
 
@@ -531,6 +531,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     __syncthreads();
   }
   const int total = cw[2];
+  if (kFromList && A.lcount[tile] != total) {  // the lists of another binning: not computed from
+    if (tid == 0) atomicOr(A.status, ST_BOUNDS);
+    return;
+  }
   if (MODE == kListBuild && (total > cap || total > A.lslots)) {  // no list: the redo pass enumerates it every step
     if (tid == 0) {
       A.lcount[tile] = -1;
@@ -593,6 +597,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     }
   }
   int* big_flag = cw + 1;  // mixed form: a term was too large for the fixed-point sums
+  // list passes: the padding entries' atom, beyond every cutoff
+  if (kFromList && tid == 0) pf[total] = make_float4(1e30f, 0.f, 0.f, 0.f);
   if (tid == 0) {
     cw[0] = 0;  // work-unit counter
     cw[3] = 0;  // list build: the tile's entries so far
@@ -896,7 +902,9 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int by = lyi * kDT + 2 - lyi, bz = lzi * kDT + 2 - lzi;  // + the j row: the row offset's entry
       // entries k..k+3 of this lane: 8 bytes at brick k / 4 of the group
       const uint2* col = reinterpret_cast<const uint2*>(lst + (size_t)g * 32 * lk) + lane;
-      auto four = [&](int k) { return k < cnt ? __ldcs(col + (size_t)(k >> 2) * 32) : make_uint2(0u, 0u); };
+      // (every lane's bricks hold entries up to the group's longest, the
+      // padding entries naming the far atom `total`: no per-lane count test)
+      auto four = [&](int k) { return k < gm ? __ldcs(col + (size_t)(k >> 2) * 32) : make_uint2(0u, 0u); };
       uint2 nxt = four(0);
       int sx = 0, sy = 0, sz = 0;  // atom i's fixed-point sums
       for (int k0 = 0; k0 < gm; k0 += 4) {
@@ -905,8 +913,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         const unsigned wv[2] = {cur.x, cur.y};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          const bool act = k0 + q < cnt;
-          const int m = act ? (int)((wv[q >> 1] >> (16 * (q & 1))) & 0xffffu) : 0;
+          const int m = (int)((wv[q >> 1] >> (16 * (q & 1))) & 0xffffu);
           const float4 pj = pf[m];
           const int wj = __float_as_int(pj.w);
           const float cy = dyt[by + ((wj >> 7) & 31)].x, cz = dzt[bz + ((wj >> 12) & 31)].x;
@@ -917,8 +924,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
           dq.w = fmaf(dq.x, dq.x, fmaf(dq.y, dq.y, dq.z * dq.z));
           const int tj = wj & 3;
           const LJ32 P = MULTI ? ljs32[ti * A.lj.nt + tj] : q32;
-          bool acc = act && dq.w <= P.rc2;
-          if (MODE == kList && act && fabsf(dq.w - P.rc2) <= kBorder * P.rc2)
+          bool acc = dq.w <= P.rc2;
+          if (MODE == kList && fabsf(dq.w - P.rc2) <= kBorder * P.rc2)
             acc = inside64(i, m, ti, tj);  // at the border: the FP64 test
           if (MODE == kListBig) {
             redo_pair(acc, dq, i | (m << 14) | (ti << 28) | (tj << 30));
@@ -1235,9 +1242,13 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     __syncthreads();
     // a lane moves its atom's entries eight at a time (16 bytes from the
     // atom's scratch row, two 8-byte bricks that the warp's lanes store side
-    // by side); entries past the count in the last bricks are never read
+    // by side); every lane fills the group's bricks up to the group's longest
+    // count, the entries past its own count naming the padding atom `total`
+    // (staged by the list passes beyond every cutoff), so that the list pass
+    // tests no per-lane count
     const size_t nbrick = (size_t)A.ntiles * A.lslots * lk / 4;
     const unsigned short* raw = A.lraw + ltile * lk;
+    (void)nbrick;
     for (int g = warp; g * 32 < total; g += nw) {
       const int p = g * 32 + lane;
       const int t = p < total ? perm[p] : 0;
@@ -1249,16 +1260,22 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const size_t b0 = (ltile + (size_t)g * 32) * lk / 4 + lane;  // brick k / 4 of this lane: b0 + (k / 4) * 32
       uint2* dst = reinterpret_cast<uint2*>(A.list);
       // 32 entries a round: the four 16-byte reads issued before the stores
+      const unsigned dd = (unsigned)total * 0x10001u;  // two padding entries
+      // word w of a 16-byte piece holds entries 2w, 2w + 1; n of the piece are the atom's
+      auto pad = [&](unsigned w, int n) { return n >= 2 ? w : (n == 1 ? (w & 0xffffu) | (dd & 0xffff0000u) : dd); };
       for (int k0 = 0; k0 < gm; k0 += 32) {
         uint4 v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = k0 + 8 * u < c ? src[(k0 >> 3) + u] : make_uint4(0u, 0u, 0u, 0u);
+        for (int u = 0; u < 4; ++u) v[u] = k0 + 8 * u < c ? src[(k0 >> 3) + u] : make_uint4(dd, dd, dd, dd);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int k = k0 + 8 * u;
-          if (k < c) {
+          if (k < gm) {
+            const int n = c - k;
+            if (n < 8) v[u] = make_uint4(pad(v[u].x, n), pad(v[u].y, n - 2), pad(v[u].z, n - 4), pad(v[u].w, n - 6));
             dst[EXAMD_IDX(b0 + (size_t)(k >> 2) * 32, nbrick, st)] = make_uint2(v[u].x, v[u].y);
-            if (k + 4 < c) dst[EXAMD_IDX(b0 + (size_t)((k >> 2) + 1) * 32, nbrick, st)] = make_uint2(v[u].z, v[u].w);
+            if (k + 4 < gm)
+              dst[EXAMD_IDX(b0 + (size_t)((k >> 2) + 1) * 32, nbrick, st)] = make_uint2(v[u].z, v[u].w);
           }
         }
       }
