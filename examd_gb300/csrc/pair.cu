@@ -535,6 +535,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     if (tid == 0) atomicOr(A.status, ST_BOUNDS);
     return;
   }
+  if (kFromList && !(A.lj.pot == EXAMD_POT_LJ || A.lj.pot == EXAMD_POT_LJ_SHIFTED || A.lj.pot == EXAMD_POT_WCA)) {
+    if (tid == 0) atomicOr(A.status, ST_PAIRFN);  // a potential the list passes do not evaluate
+    return;
+  }
   if (MODE == kListBuild && (total > cap || total > A.lslots)) {  // no list: the redo pass enumerates it every step
     if (tid == 0) {
       A.lcount[tile] = -1;
@@ -885,6 +889,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     const unsigned short* perm = A.lperm + ltile;
     const unsigned short* cnts = A.lcnt + ltile;
     const int ng = (total + 31) >> 5;
+    bool bigl = false, perr = false;  // a large term left out; a pair-function error
     while (true) {
       int g = 0;
       if (lane == 0) g = atomicAdd(ucnt, 1);
@@ -929,30 +934,37 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
             acc = inside64(i, m, ti, tj);  // at the border: the FP64 test
           if (MODE == kListBig) {
             redo_pair(acc, dq, i | (m << 14) | (ti << 28) | (tj << 30));
-          } else if (acc) {
-            float dg = 0.f, en = 0.f;
-            const int rv = pair_fn32<ENERGY>(A.lj.pot, dq.w, P, dg, en);
-            if (rv == 0) {
-              if (ENERGY) {
-                ek.add(en);
-                wk.add(-dg * dq.w);
-              }
-              if (dq.w < P.r2big) {
-                *big_flag = 1;  // left to the redo pass
-              } else {
-                const float dgs = kFix * dg;
-                const int ix = __float2int_rn(dgs * dq.x), iy = __float2int_rn(dgs * dq.y),
-                          iz = __float2int_rn(dgs * dq.z);
-                atomicAdd(&fa[m], -ix);
-                atomicAdd(&fa[cap + m], -iy);
-                atomicAdd(&fa[2 * cap + m], -iz);
-                sx += ix;
-                sy += iy;
-                sz += iz;
-              }
-            } else if (rv < 0) {
-              atomicOr(A.status, ST_PAIRFN);
+          } else {
+            // The LJ family's expression of pair_fn32 (the potential was
+            // checked per tile) for every entry, its result kept where the
+            // entry applies: some lane of the warp takes nearly every entry,
+            // so a branch would only add reconvergence, and without it the
+            // four entries' arithmetic interleaves.  The same expressions:
+            // the same bits as pair_fn32 where it applies.
+            const float ri = rcp_approx(dq.w);
+            const float s2 = P.sig2 * ri;
+            const float s6 = s2 * s2 * s2;
+            const float dg = P.m24eps * s6 * fmaf(2.f, s6, -1.f) * ri;
+            perr |= acc && !(dq.w >= kR2Min32);  // pair_fn32's error return
+            const bool app = acc && dq.w >= kR2Min32 && !(dq.w > P.rcut2);
+            if (ENERGY && app) {
+              ek.add(P.c4eps * s6 * (s6 - 1.f) - P.eshift);
+              wk.add(-dg * dq.w);
             }
+            const bool big = app && dq.w < P.r2big;  // left to the redo pass
+            bigl |= big;
+            const bool fix = app && !big;
+            const float dgs = fix ? kFix * dg : 0.f;
+            const int ix = __float2int_rn(dgs * dq.x), iy = __float2int_rn(dgs * dq.y),
+                      iz = __float2int_rn(dgs * dq.z);
+            if (fix) {
+              atomicAdd(&fa[m], -ix);
+              atomicAdd(&fa[cap + m], -iy);
+              atomicAdd(&fa[2 * cap + m], -iz);
+            }
+            sx += ix;
+            sy += iy;
+            sz += iz;
           }
         }
       }
@@ -962,6 +974,8 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
         atomicAdd(&fa[2 * cap + i], sz);
       }
     }
+    if (bigl) *big_flag = 1;
+    if (perr) atomicOr(A.status, ST_PAIRFN);
   } else if constexpr (!FP64) {
     // ---- item building: (staged atom, owned row) pairs, laid end to end ----
     // A unit is 32 consecutive staged atoms and one of kParts shares of each
