@@ -457,6 +457,7 @@ int examd_gpu_create(const examd_params* params, int nboxes, const examd_box* bo
   // pair-kernel configuration
   ctx->pc.fp64 = p.precision == EXAMD_FP64;
   ctx->pc.multi = nt > 1;
+  ctx->pc.cut = p.potential == EXAMD_POT_WCA;
   ctx->pc.pack = p.pair_tables == 2;
   ctx->pair_tables = p.pair_tables;
   if (p.pair_tables < 0 || p.pair_tables > 2 || p.tile_balance < 0 || p.tile_balance > 1) {

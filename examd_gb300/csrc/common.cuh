@@ -101,9 +101,10 @@ struct BoxDev {
 // own range (<= rc2; FP32 table: infinite where it is rc2, which the
 // candidate test decides); eshift: subtracted from the pair energy.
 struct LJ32 {
-  float sig2, m24eps, c4eps, rc2;  // m24eps = -24 eps (dg prefactor)
-  float rcut2, eshift;
+  // the fields every list entry reads first, in one 16-byte word
+  float sig2, m24eps, rc2;  // m24eps = -24 eps (dg prefactor)
   float r2big;  // r^2 below which |F| >= kFixMaxForce (mixed form: left to the redo pass)
+  float c4eps, eshift, rcut2;
   float rl2;    // pair-list mode: (rc + skin)^2, the list's cutoff for this type pair
 };
 

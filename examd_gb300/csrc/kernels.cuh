@@ -97,6 +97,7 @@ struct PairConfig {
   bool energy = false;  // potential energy and virial
   bool count = false;   // candidate / accepted counters
   bool list = false;    // mixed form: pair-list mode (forces from the per-tile lists)
+  bool cut = true;      // list pass: the potential's own range is finite (WCA) and tested
   int warps = 8;
 };
 

@@ -395,7 +395,8 @@ __device__ __forceinline__ void force_batch64(int cnt, const QK& qk, const PD& p
 //   expressions as the first pass (the same bits when the atoms are where
 //   the list was built), outputs, energy and the large-term flag as there;
 // - kListBig: kRedoBig from the list.
-template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, int MODE, bool PACK>
+// CUT (list pass): the potential's own range rcut2 is tested (WCA; infinite otherwise).
+template <bool FP64, bool MULTI, bool ENERGY, bool COUNT, int MODE, bool PACK, bool CUT = true>
 __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned FULL = 0xffffffffu;
@@ -946,7 +947,7 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
             const float s6 = s2 * s2 * s2;
             const float dg = P.m24eps * s6 * fmaf(2.f, s6, -1.f) * ri;
             perr |= acc && !(dq.w >= kR2Min32);  // pair_fn32's error return
-            const bool app = acc && dq.w >= kR2Min32 && !(dq.w > P.rcut2);
+            const bool app = acc && dq.w >= kR2Min32 && !(CUT && dq.w > P.rcut2);
             if (ENERGY && app) {
               ek.add(P.c4eps * s6 * (s6 - 1.f) - P.eshift);
               wk.add(-dg * dq.w);
@@ -1411,9 +1412,9 @@ __global__ void __launch_bounds__(256, FP64 ? 3 : 4) k_pair(const PairArgs A) {
 
 // Pair-list mode: the forces of every tile from its list (fallback tiles
 // return at once: the redo pass enumerates them).
-template <bool MULTI, bool ENERGY>
+template <bool MULTI, bool ENERGY, bool CUT>
 __global__ void __launch_bounds__(256, 4) k_pair_list(const PairArgs A) {
-  pair_tile<false, MULTI, ENERGY, false, kList, false>(A, A.order[blockIdx.x]);
+  pair_tile<false, MULTI, ENERGY, false, kList, false, CUT>(A, A.order[blockIdx.x]);
 }
 
 // Pair-list mode: the lists of every tile, on the steps whose gate is set.
@@ -1484,8 +1485,12 @@ static bool uses_list(const PairConfig& c) { return c.list && !c.fp64 && !c.coun
 
 static void* pick(const PairConfig& c) {
   if (uses_list(c)) {
-    if (c.multi) return c.energy ? (void*)&k_pair_list<true, true> : (void*)&k_pair_list<true, false>;
-    return c.energy ? (void*)&k_pair_list<false, true> : (void*)&k_pair_list<false, false>;
+    if (c.cut) {
+      if (c.multi) return c.energy ? (void*)&k_pair_list<true, true, true> : (void*)&k_pair_list<true, false, true>;
+      return c.energy ? (void*)&k_pair_list<false, true, true> : (void*)&k_pair_list<false, false, true>;
+    }
+    if (c.multi) return c.energy ? (void*)&k_pair_list<true, true, false> : (void*)&k_pair_list<true, false, false>;
+    return c.energy ? (void*)&k_pair_list<false, true, false> : (void*)&k_pair_list<false, false, false>;
   }
   return pick_enum(c);
 }
