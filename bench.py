@@ -520,6 +520,7 @@ def main():
     sysm.forces_at(hp, out=hf)  # the captured call, at both parities of the sort's double buffer
     e2e_steps = max(args.steps // 2, 10)
     t_e2e = 0.0
+    builds0 = sysm.list_info()["builds"] if skin > 0 else 0
     for k in range(e2e_steps):
         hp[:] = states[k % nstate]
         barrier(dist)
@@ -528,6 +529,7 @@ def main():
         t_e2e += time.perf_counter() - t0
     t_e2e = allmax(dist, t_e2e)
     e2e = n * e2e_steps * ws / t_e2e
+    e2e_rebuilds = sysm.list_info()["builds"] - builds0 if skin > 0 else 0
     phases = sysm.time_phases(10, dt)  # advances the state: last
     sysm.close()
 
@@ -538,7 +540,8 @@ def main():
             "clocks": clk.summary(),
             "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
                     "call": "examd_gpu_forces_at (positions in, forces out, pinned host buffers), "
-                            f"positions of {nstate} consecutive steps in turn, each call timed"},
+                            f"positions of {nstate} consecutive steps in turn, each call timed",
+                    "calls": e2e_steps, "list_rebuilds_in_calls": e2e_rebuilds},
             # per step: kick+drift+bin count, 2 scan kernels, finalize, pair, redo pass (pair lists: kick, the
             # rebuild decision, bin count, 2 scan kernels, finalize, copy-back and list build, which return at
             # once on a step that does not rebuild, list pass, redo pass); + the closing kick
