@@ -72,7 +72,10 @@ struct PairArgs {
   // counts in that order (lcnt); the entries, the staged indices m of the
   // pairs (i, m) that the tile owns within the list cutoff, in that order by
   // groups of 32 atoms, entries k..k+3 of the group's 32 atoms side by side
-  // (list[tile][p / 32][k / 4][p % 32][k % 4] for the atom at position p);
+  // (list[tile][p / 32][k / 4][p % 32][k % 4] for the atom at position p),
+  // every atom's entries padded up to its group's longest count with the
+  // tile's staged-atom count (an index the list passes stage beyond every
+  // cutoff);
   // the build's scratch, each atom's entries in staged order
   // (lraw[tile][i][k]); per tile the staged atoms, or -1 when the tile is in
   // the fallback list fb (computed by enumeration every step); the list
