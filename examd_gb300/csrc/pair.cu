@@ -43,6 +43,7 @@
 // the partial slot P[s] (s = bitmask of the axes on which the copy is a halo
 // copy); the integrator sums an atom's 1..8 partials in a fixed order.
 #include <algorithm>
+#include <type_traits>
 
 #include <cuda_fp16.h>
 
@@ -891,6 +892,16 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
     const unsigned short* cnts = A.lcnt + ltile;
     const int ng = (total + 31) >> 5;
     bool bigl = false, perr = false;  // a large term left out; a pair-function error
+    // The origin offset between rows l and l + d (d = -2..2 for a listed
+    // pair) is fmaf(image difference, r, d bl) in the tables: d bl itself
+    // (exact) unless the tile reaches the box's periodic face on that axis
+    // and the box's last cell is wider by r != 0.  Such tiles read the
+    // tables; the others form d bl in registers, the same bits.
+    const bool taby = B.remf[1] != 0.f && (Y0 == 0 || Y0 + ty >= B.nb[1]);
+    const bool tabz = B.remf[2] != 0.f && (Z0 == 0 || Z0 + tz >= B.nb[2]);
+    const float blf = B.blf;
+    // d as a float, exactly, without a conversion instruction (|d| < 2^22)
+    auto dfloat = [](int d) { return __fsub_rn(__int_as_float(0x4B400000 + d), 12582912.f); };
     while (true) {
       int g = 0;
       if (lane == 0) g = atomicAdd(ucnt, 1);
@@ -905,7 +916,6 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       const int wi = __float_as_int(pi.w);
       const int ti = wi & 3;
       const int lyi = (wi >> 7) & 31, lzi = (wi >> 12) & 31;
-      const int by = lyi * kDT + 2 - lyi, bz = lzi * kDT + 2 - lzi;  // + the j row: the row offset's entry
       // entries k..k+3 of this lane: 8 bytes at brick k / 4 of the group
       const uint2* col = reinterpret_cast<const uint2*>(lst + (size_t)g * 32 * lk) + lane;
       // (every lane's bricks hold entries up to the group's longest, the
@@ -913,6 +923,10 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
       auto four = [&](int k) { return k < gm ? __ldcs(col + (size_t)(k >> 2) * 32) : make_uint2(0u, 0u); };
       uint2 nxt = four(0);
       int sx = 0, sy = 0, sz = 0;  // atom i's fixed-point sums
+      // the entries, in one of two versions: row offsets from the tables or
+      // formed in registers (no table load)
+      auto walk = [&](auto tables) {
+      constexpr bool TAB = decltype(tables)::value;
       for (int k0 = 0; k0 < gm; k0 += 4) {
         const uint2 cur = nxt;
         nxt = four(k0 + 4);
@@ -922,7 +936,16 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
           const int m = (int)((wv[q >> 1] >> (16 * (q & 1))) & 0xffffu);
           const float4 pj = pf[m];
           const int wj = __float_as_int(pj.w);
-          const float cy = dyt[by + ((wj >> 7) & 31)].x, cz = dzt[bz + ((wj >> 12) & 31)].x;
+          const int lyj = (wj >> 7) & 31, lzj = (wj >> 12) & 31;
+          // (the table entry of rows l, l + d: l kDT + d + 2)
+          float cy, cz;
+          if constexpr (TAB) {
+            cy = dyt[lyi * (kDT - 1) + 2 + lyj].x;
+            cz = dzt[lzi * (kDT - 1) + 2 + lzj].x;
+          } else {
+            cy = __fmul_rn(dfloat(lyj - lyi), blf);
+            cz = __fmul_rn(dfloat(lzj - lzi), blf);
+          }
           float4 dq;
           dq.x = pj.x + (-pi.x);
           dq.y = pj.y + (cy - pi.y);
@@ -969,6 +992,11 @@ __device__ __forceinline__ void pair_tile(const PairArgs& A, const int tile) {
           }
         }
       }
+      };
+      if (taby || tabz)
+        walk(std::true_type{});
+      else
+        walk(std::false_type{});
       if (MODE == kList && (sx | sy | sz) != 0) {
         atomicAdd(&fa[i], sx);
         atomicAdd(&fa[cap + i], sy);
